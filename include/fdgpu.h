@@ -1,0 +1,121 @@
+/*
+ * fdgpu.h — C ABI of the GB300 sphfd travel-time solver (libfdgpu.so).
+ *
+ * The library replaces the solve of FDtomoC's sphfd program (reference: src/sphfd.c).  Its
+ * results are bit-identical to the reference's: same travel times, same head-wave restarts.
+ *
+ * Two levels:
+ *   1. Drop-in entry points with the reference's file interface:
+ *        fdgpu_sphfd          replaces  int sphfd(int ac, char **av, char *output_path)
+ *                                       (src/sphfd.c:194, body :260-5803)
+ *        fdgpu_sphfd_parlist  replaces  the OpenMP loop over par files in main()
+ *                                       (src/sphfd.c:247-255); all stations run on the GPU at once.
+ *   2. Array entry points for callers that keep models and fields in memory (the batch and
+ *      serving drivers): fdgpu_station_from_par, fdgpu_solve_host, fdgpu_solve_device.
+ *
+ * Conventions: every function returns an FDGPU_* status (0 = success) and never aborts; the
+ * caller owns host buffers and any device buffers it passes in; the library owns its scratch,
+ * geometry tables and streams, all held in an fdgpu_ctx.  A context is not thread-safe; use one
+ * per host thread.  Grids are x fastest (index nx*ny*z + nx*y + x), as in the reference.
+ */
+#ifndef FDGPU_H
+#define FDGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    FDGPU_OK = 0,
+    FDGPU_EINVAL = -1,   /* bad argument */
+    FDGPU_ENOMEM = -2,   /* device or host allocation failed */
+    FDGPU_ECUDA = -3,    /* a CUDA call failed (message via fdgpu_last_error) */
+    FDGPU_EIO = -4,      /* a file could not be read or written */
+    FDGPU_EPAR = -5,     /* a required par parameter is missing or a value is invalid */
+    FDGPU_ESOURCE = -6,  /* the source is outside the grid (src/sphfd.c:533-538) */
+    FDGPU_ESCHED = -7,   /* internal: a face walk exceeded its round bound */
+    FDGPU_ENODEV = -8    /* no CUDA device */
+};
+
+typedef struct fdgpu_ctx fdgpu_ctx;
+
+/* One station solve, as sphfd() has set it up after reading its par file (src/sphfd.c:383-552,
+ * 724-825, 977-1003).  fdgpu_station_from_par fills it from par-file arguments. */
+typedef struct {
+    int nx, ny, nz;
+    double h;              /* radial step, km */
+    double dq, df;         /* colatitude / longitude steps, radians */
+    double x0;             /* longitude of x = 0, radians */
+    double y0;             /* geocentric colatitude of y = 0, radians */
+    double z0r;            /* radius of z = 0, km */
+    int srctype;           /* 1 point source; 3 restart from a supplied field (srcwall); 2 as 3 */
+    int xs, ys, zs;        /* source node (srctype 1) */
+    double src_geo[3];     /* geocentric source: longitude rad, colatitude rad, radius km */
+    int ncube;             /* source box half-width (NCUBE) */
+    int reverse;           /* up to reverse+1 sweeps */
+    int headpref;          /* par value (> 0: prefer the wall opposite the source) */
+    int maxrad;            /* radius limit from maxoff (99999999 = none) */
+    int kminus, kplus, iplus, iminus, jminus, jplus;
+    int srcwall;           /* srctype 2/3: wall holding the starting times (1..6) */
+    int ox, oy, oz;        /* this grid's origin inside the slowness model it reads */
+} fdgpu_station;
+
+typedef struct {
+    int32_t status;
+    int32_t sweeps;          /* sweeps run (1 + restarts) */
+    int64_t node_updates;    /* face-point evaluations */
+    int64_t faces;
+    int64_t rounds;          /* dependency rounds of the face walks */
+    int64_t deferred;        /* points that took the stale (t0,t4) of an earlier point */
+    int64_t stencils[5];     /* stencil evaluations: 3-D, new-edge, 2-D, new-face, 1-D */
+    int32_t restart_wall[8]; /* restarts per wall 1..6 */
+} fdgpu_stats;
+
+int fdgpu_create(int device, fdgpu_ctx **out);
+void fdgpu_destroy(fdgpu_ctx *ctx);
+const char *fdgpu_strerror(int status);
+/* text of the last CUDA or I/O failure in this context ("" if none) */
+const char *fdgpu_last_error(const fdgpu_ctx *ctx);
+
+/* Parse getpar-style arguments (e.g. {"sphfd", "par=station.par"}) the way sphfd() does
+ * (src/sphfd.c:383-552): geometry conversion (WGS84 geocentric colatitude), source placement,
+ * box walls.  velfile/timefile receive the file names from the par file (timefile without the
+ * output directory).  Replaces the set-up part of sphfd(). */
+int fdgpu_station_from_par(int ac, char **av, fdgpu_station *st, char *velfile, size_t velcap,
+                           char *timefile, size_t timecap);
+
+/* Solve n stations whose velocities are in host memory: model (mnx, mny, mnz) is copied to the
+ * device, converted to slowness, each station reads its window at (ox, oy, oz), and each field is
+ * copied back to times[k] (nx*ny*nz floats).  init_times[k] may give the starting field for
+ * srctype 2/3 stations (NULL otherwise).  stats may be NULL. */
+int fdgpu_solve_host(fdgpu_ctx *ctx, int n, const fdgpu_station *st, const float *velocity, int mnx, int mny,
+                     int mnz, float *const *times, const float *const *init_times, fdgpu_stats *stats);
+
+/* Same with everything already on the device: slowness (1/v, float) of a model with strides
+ * (1, s_sy, s_sz), one device field per station.  Work is queued on `stream` (a cudaStream_t,
+ * NULL = the context's stream); the call returns after the solve has completed. */
+int fdgpu_solve_device(fdgpu_ctx *ctx, int n, const fdgpu_station *st, const float *slowness, long long s_sy,
+                       long long s_sz, float *const *d_times, int times_initialised, fdgpu_stats *stats,
+                       void *stream);
+
+/* velocity -> slowness on the device, slow[i] = 1/v[i] as the reference rounds it (src/sphfd.c:689) */
+int fdgpu_velocity_to_slowness(fdgpu_ctx *ctx, const float *d_velocity, float *d_slowness, long long n,
+                               void *stream);
+
+/* Drop-in sphfd(): ac/av as the reference's (av[1] = "par=<file>"), output_path = timedir.
+ * Reads the velocity file, solves on the GPU, writes <output_path>/<timefile> byte-for-byte as
+ * the reference does.  Uses a per-thread default context on device 0. */
+int fdgpu_sphfd(int ac, char **av, const char *output_path);
+
+/* Drop-in for main()'s loop over a par list: every entry is "par=<file>"; all stations are solved
+ * together (stations sharing a velocity file share one device copy).  status[k] receives each
+ * station's result if status is non-NULL; the return value is the first failure (or 0). */
+int fdgpu_sphfd_parlist(int n, char **par_entries, const char *output_path, int *status);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
