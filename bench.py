@@ -1,0 +1,395 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 sphfd travel-time solver.
+
+Metric: station travel-time fields per second (with node-updates/s), batched, on the 64-station
+201x201x81 workload (0.005 deg x 0.005 deg x 0.5 km, layered 1-D model with a 5 % / 10 km
+perturbation, seed 2; stations on the surface with 0-2 km elevation).  One step = one batch of
+64 station solves.  Every GPU field is bit-identical to the CPU oracle (checked here on the
+stations the CPU baseline solves).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W]     GPU arm (torchrun for N > 1)
+  python bench.py --impl reference ...                     CPU arm: the oracle on the host cores
+
+The reference repository has no GPU code; the CPU arm runs this repository's C restatement of
+its solver (oracle/, pinned bit-exact against the reference's own binary and golden file) on all
+host cores, one process per core, as the reference's OpenMP driver does.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import shutil
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "station fields/s (batched, 201x201x81, bit-identical to reference)"
+UNIT = "station fields/s"
+STATIONS_PER_GPU = 64
+CONFIG_NAME = "64 stations, 201x201x81 grid, 0.005deg x 0.005deg x 0.5km (config 2)"
+ALGO_BYTES_PER_NODE_UPDATE = 12  # slowness read, time read, time write
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--stations", type=int, default=STATIONS_PER_GPU)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
+            int(os.environ.get("LOCAL_RANK", 0)))
+
+
+def workload(rank: int, n: int):
+    """The config-2 model and this rank's n stations (weak scaling: rank r takes its own stations)."""
+    from fdtomoc_gb300 import workloads as W
+    g, v, _ = W.config(2)
+    sts = W.stations(g, n * (rank + 1), 2)[n * rank:]
+    return g, v, sts
+
+
+def write_case(dirname, g, v, sts):
+    from fdtomoc_gb300 import workloads as W
+    return W.write_case(dirname, g, v, sts)
+
+
+# ----------------------------------------------------------------------------------------------
+# CPU side: the oracle, one process per core
+
+
+def build_oracle():
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "liboracle.so", "sphfd_oracle"], check=True)
+    return os.path.join(ROOT, "oracle", "sphfd_oracle")
+
+
+def cpu_solve(case_dir, names, cores, mode="fast"):
+    """Solve the named stations with the oracle, one process per core; returns (wall s, node updates)."""
+    exe = build_oracle()
+    out = os.path.join(case_dir, "cpu_out")
+    os.makedirs(out, exist_ok=True)
+    procs = []
+    env = dict(os.environ, FDO_MODE=mode, OMP_NUM_THREADS="1")
+    t0 = time.time()
+    pending = list(names)
+    running = []
+    logs = {}
+    while pending or running:
+        while pending and len(running) < cores:
+            nm = pending.pop(0)
+            pl = os.path.join(case_dir, f"pl_{nm}")
+            with open(pl, "w") as f:
+                f.write(f"par={os.path.join(case_dir, nm + '.par')}\n")
+            spec = os.path.join(case_dir, f"spec_{nm}")
+            with open(spec, "w") as f:
+                f.write(f"parlist {pl}\ntimedir {out}\n")
+            p = subprocess.Popen([exe], stdin=subprocess.PIPE, stdout=subprocess.DEVNULL, stderr=subprocess.PIPE,
+                                 text=True, env=env)
+            p.stdin.write(spec + "\n")
+            p.stdin.close()
+            running.append((nm, p))
+        time.sleep(0.02)
+        still = []
+        for nm, p in running:
+            if p.poll() is None:
+                still.append((nm, p))
+            else:
+                logs[nm] = p.stderr.read()
+                if p.returncode != 0:
+                    raise RuntimeError(f"oracle failed on {nm}: {logs[nm]}")
+        running = still
+    wall = time.time() - t0
+    nu = 0
+    for nm in names:
+        for tok in logs[nm].split():
+            if tok.startswith("node_updates="):
+                nu += int(tok.split("=")[1])
+    return wall, nu, out
+
+
+# ----------------------------------------------------------------------------------------------
+# clocks sampled during the timed region
+
+
+class ClockSampler:
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        if not shutil.which("nvidia-smi"):
+            return
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits", "-lms", "200",
+                                      "-i", str(self.index)], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, val in zip(["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"], f[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "samples": len(sm), "reasons": sorted(reasons)}
+
+
+# ----------------------------------------------------------------------------------------------
+# GPU arm
+
+
+def run_gpu(args):
+    rank, world, local = dist_env()
+    n = args.stations
+    case_dir = tempfile.mkdtemp(prefix=f"fdbench_r{rank}_")
+    g, v, sts = workload(rank, n)
+    write_case(case_dir, g, v, sts)
+    names = [s["name"] for s in sts]
+
+    # CPU baseline first (before any CUDA call in this process), rank 0 at N=1 only
+    cpu = None
+    ncores = os.cpu_count() or 1
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        sample = names[:min(ncores, n)]
+        wall, nu_cpu, cpu_out = cpu_solve(case_dir, sample, ncores)
+        cpu = dict(value=len(sample) / wall, unit=UNIT, cores=min(ncores, len(sample)), kind="port",
+                   sample=f"{len(sample)} of the {n} stations, one oracle process per core (oracle FAST mode: "
+                          f"exact pruned restatement, faster than the reference binary), {wall:.1f} s wall",
+                   node_updates_per_s=nu_cpu / wall)
+
+    import numpy as np
+    import torch
+    from fdtomoc_gb300 import build, lib
+
+    build.build()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    stations = [lib.station_from_par("par=" + os.path.join(case_dir, nm + ".par"))[0] for nm in names]
+    ctx = lib.Context(local)
+    stream = torch.cuda.Stream()
+    vel_d = torch.from_numpy(v.reshape(-1)).cuda()
+    slow = torch.empty_like(vel_d)
+    with torch.cuda.stream(stream):
+        ctx.velocity_to_slowness(vel_d.data_ptr(), slow.data_ptr(), v.size, stream.cuda_stream)
+    stream.synchronize()
+    fields = [torch.empty(s.shape, dtype=torch.float32, device="cuda") for s in stations]
+    tptr = [f.data_ptr() for f in fields]
+
+    def step():
+        return ctx.solve_device(stations, slow.data_ptr(), g.nx, g.nx * g.ny, tptr, stream_ptr=stream.cuda_stream)
+
+    for _ in range(args.warmup):
+        stats = step()
+
+    # parity against the CPU oracle on the stations it solved
+    parity = None
+    if cpu is not None:
+        nd, maxd = 0, 0.0
+        for nm, f in zip(names[:cpu["cores"]], fields):
+            ref = np.fromfile(os.path.join(case_dir, "cpu_out", nm + ".ptimes"), dtype="<f4", offset=232)
+            got = f.cpu().numpy().reshape(-1)
+            nd += int((ref != got).sum())
+            maxd = max(maxd, float(np.abs(ref.astype(np.float64) - got).max()))
+        parity = {"stations_checked": cpu["cores"], "nodes_differing": nd, "max_abs_dt_s": maxd,
+                  "tolerance_s": 1e-4, "bit_identical": nd == 0}
+
+    # timed region
+    sampler = ClockSampler(local)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    sampler.start()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    all_stats = []
+    for _ in range(args.steps):
+        all_stats.append(step())
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clocks = sampler.stop()
+    ms = ev0.elapsed_time(ev1)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_step = ms / args.steps
+    total_stations = n * world
+    value = total_stations * args.steps / (ms / 1e3)
+    nu_step = sum(s["node_updates"] for s in all_stats[-1])
+    lat = sorted((s["t_end_ns"] - min(x["t_start_ns"] for x in all_stats[-1])) / 1e6 for s in all_stats[-1])
+    p50 = lat[len(lat) // 2]
+    p99 = lat[min(len(lat) - 1, int(round(0.99 * (len(lat) - 1))))]
+
+    # plain form: one station per launch
+    t0 = time.time()
+    ev0.record(stream)
+    ctx.solve_device(stations[:1], slow.data_ptr(), g.nx, g.nx * g.ny, tptr[:1], stream_ptr=stream.cuda_stream)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    plain_ms = ev0.elapsed_time(ev1)
+
+    # end to end through the host-buffer entry point: pinned velocity in, all fields out
+    vel_h = torch.from_numpy(v.reshape(-1).copy()).pin_memory()
+    outs = [torch.empty(s.shape, dtype=torch.float32).pin_memory() for s in stations]
+    import ctypes as C
+    lib_ = lib.load()
+    arr = (lib.Station * n)(*stations)
+    outp = (C.POINTER(C.c_float) * n)(*[C.cast(o.data_ptr(), C.POINTER(C.c_float)) for o in outs])
+    e2e_steps = max(1, min(args.steps, 2))
+    rc = lib_.fdgpu_solve_host(ctx.ptr, n, arr, C.cast(vel_h.data_ptr(), C.POINTER(C.c_float)), g.nx, g.ny, g.nz,
+                               outp, None, None)   # warm-up: allocates the context's host-path buffers
+    if rc != 0:
+        raise RuntimeError(f"fdgpu_solve_host failed: {rc}")
+    torch.cuda.synchronize()
+    t0 = time.time()
+    for _ in range(e2e_steps):
+        rc = lib_.fdgpu_solve_host(ctx.ptr, n, arr, C.cast(vel_h.data_ptr(), C.POINTER(C.c_float)), g.nx, g.ny,
+                                   g.nz, outp, None, None)
+        if rc != 0:
+            raise RuntimeError(f"fdgpu_solve_host failed: {rc}")
+    e2e_s = (time.time() - t0) / e2e_steps
+    e2e = {"value": total_stations / e2e_s if world == 1 else None, "unit": UNIT,
+           "h2d_bytes_per_step": int(v.size * 4), "d2h_bytes_per_step": int(sum(o.numel() * 4 for o in outs))}
+    if world > 1:
+        t = torch.tensor([e2e_s], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e["value"] = total_stations / float(t.item())
+
+    # roofline of the solve kernel (one launch per step): algorithmic bytes 12 B per node update
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    peak = peaks.get("hbm_gbs", 6800.0)
+    achieved = ALGO_BYTES_PER_NODE_UPDATE * nu_step / (ms_step / 1e3) / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "fd_solve_traffic.json")
+    if os.path.exists(tpath):
+        tj = json.load(open(tpath))
+        traffic = tj["dram_bytes_per_node_update"] * nu_step
+    # FP64 pipe roofline: FP64 instructions per stencil evaluation (static counts of the evaluators,
+    # divisions 5, square roots 8) x evaluations, against the FP64 rate measured live on this GPU
+    st_sum = [sum(s["stencils"][k] for s in all_stats[-1]) for k in range(5)]
+    fp64_ops = 116 * st_sum[0] + 70 * st_sum[1] + 69 * st_sum[2] + 25 * st_sum[3] + 6 * st_sum[4]
+    fp64_peak = ctx.probe_fp64_gops()
+    fp64 = {"achieved_gops": fp64_ops / (ms_step / 1e3) / 1e9, "peak_gops": fp64_peak,
+            "frac": fp64_ops / (ms_step / 1e3) / 1e9 / fp64_peak, "peak_kind": "measured (FP64 add/mul/fma chain probe)"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64 stencils / f32 fields", "data": "synthetic (seeded, config 2 recipe)",
+            "config": {"workload": CONFIG_NAME, "stations_per_gpu": n, "grid": [g.nx, g.ny, g.nz],
+                       "l2": "inputs larger than L2 (64 fields x 13 MB + 13 MB model)", "parallelism": f"stations x{world}"},
+            "node_updates_per_s": nu_step * world / (ms_step / 1e3),
+            "latency_ms": {"p50": p50, "p99": p99, "what": "station completion time within a batch"},
+            "plain": {"ms_per_station": plain_ms, "fields_per_s": 1e3 / plain_ms,
+                      "batched_over_plain": value / world / (1e3 / plain_ms)},
+            "e2e": e2e,
+            "gpu_launches": args.steps,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": traffic, "note": "the path is FP64- and dependency-latency-bound, not HBM-bound"},
+            "fp64": fp64,
+            "parity": parity,
+            "clocks": clocks,
+            "sweeps": [s["sweeps"] for s in all_stats[-1]][:8],
+        }
+        if cpu is not None:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    shutil.rmtree(case_dir, ignore_errors=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+# ----------------------------------------------------------------------------------------------
+# reference arm: the oracle on the host cores
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    n = args.stations
+    ncores = os.cpu_count() or 1
+    case_dir = tempfile.mkdtemp(prefix="fdbench_ref_")
+    g, v, sts = workload(0, n)
+    write_case(case_dir, g, v, sts)
+    names = [s["name"] for s in sts]
+    sample = names[:min(ncores, n)]
+    for _ in range(args.warmup):
+        cpu_solve(case_dir, sample, ncores)
+    walls, nus = [], []
+    for k in range(args.steps):
+        wall, nu, _ = cpu_solve(case_dir, sample, ncores)
+        walls.append(wall)
+        nus.append(nu)
+    tot = sum(walls)
+    value = len(sample) * args.steps / tot
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64 stencils / f32 fields", "data": "synthetic (seeded, config 2 recipe)",
+        "config": {"workload": CONFIG_NAME, "stations_per_gpu": n, "grid": [g.nx, g.ny, g.nz],
+                   "parallelism": f"{len(sample)} processes x 1 thread"},
+        "node_updates_per_s": sum(nus) / tot,
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": len(sample), "kind": "port",
+                         "sample": f"{len(sample)} of the {n} stations per step, one oracle process per core "
+                                   "(oracle FAST mode, exact)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    shutil.rmtree(case_dir, ignore_errors=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

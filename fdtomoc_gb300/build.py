@@ -41,8 +41,12 @@ def _stale(out, srcs):
     return any(os.path.getmtime(s) > t for s in srcs)
 
 
-def build(force: bool = False, verbose: bool = False) -> str:
+def build(force: bool = False, verbose: bool = False, defines=(), lib_path: str | None = None) -> str:
+    """Compile the library.  `defines` (e.g. ["FDGPU_PHASE_TIMERS"]) and `lib_path` build a
+    separately named profiling variant."""
     nvcc = _nvcc()
+    lib_out = lib_path or LIB
+    tag = "_".join(defines)
     os.makedirs(BUILD, exist_ok=True)
     os.makedirs(os.path.dirname(EXE), exist_ok=True)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
@@ -52,16 +56,18 @@ def build(force: bool = False, verbose: bool = False) -> str:
     jobs = []
     for src, extra in units:
         s = os.path.join(CSRC, src)
-        o = os.path.join(BUILD, src + ".o")
+        o = os.path.join(BUILD, src + (("." + tag) if tag else "") + ".o")
         objs.append(o)
         if force or _stale(o, [s] + headers):
-            jobs.append([nvcc] + ARCH + NVFLAGS + extra + ["-c", s, "-o", o])
+            jobs.append([nvcc] + ARCH + NVFLAGS + extra + ["-D" + d for d in defines] + ["-c", s, "-o", o])
     with cf.ThreadPoolExecutor(max_workers=4) as ex:
         for r in ex.map(_run, jobs):
             if verbose:
                 print(r.stderr)
-    if force or _stale(LIB, objs):
-        _run([nvcc] + ARCH + ["-shared", "-cudart", "static", "-o", LIB] + objs)
+    if force or _stale(lib_out, objs):
+        _run([nvcc] + ARCH + ["-shared", "-cudart", "static", "-o", lib_out] + objs)
+    if lib_path:
+        return lib_out
     main = os.path.join(CSRC, "sphfd_main.cpp")
     if force or _stale(EXE, [main, LIB]):
         _run([nvcc] + ARCH + NVFLAGS + [main, "-o", EXE, "-L" + HERE, "-lfdgpu", "-Xlinker", "-rpath=" + HERE])

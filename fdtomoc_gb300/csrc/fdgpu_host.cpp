@@ -26,8 +26,10 @@
 extern "C" cudaError_t fdk_launch_geo_build(int nx, int ny, int nz, double h, double dq, double df, double z0r,
                                             const double *ysin, double *zrow, double *node, double *cell,
                                             cudaStream_t stream);
-extern "C" cudaError_t fdk_launch_solve(const fd_station_dev *stations, int nst, cudaStream_t stream);
+extern "C" cudaError_t fdk_launch_solve(const fd_station_dev *stations, int nst, long long max_face_pad,
+                                        cudaStream_t stream);
 extern "C" cudaError_t fdk_launch_v2s(const float *v, float *s, long long n, cudaStream_t stream);
+extern "C" cudaError_t fdk_probe_fp64(double *scratch, int blocks, int threads, int iters, float *ms, cudaStream_t s);
 
 namespace {
 
@@ -187,7 +189,7 @@ long long max_face(const fdgpu_station &s)
     return std::max({(long long)s.nx * s.ny, (long long)s.nx * s.nz, (long long)s.ny * s.nz});
 }
 
-constexpr size_t kScratchPerPoint = 8 + 4 + 4 + 4 + 8 + 4;
+constexpr size_t kScratchPerPoint = 8 + 4 + 4 + 4 + 8 + 4 + 2;
 
 int check_station(const fdgpu_station &s)
 {
@@ -254,6 +256,21 @@ extern "C" const char *fdgpu_strerror(int s)
 
 extern "C" const char *fdgpu_last_error(const fdgpu_ctx *ctx) { return ctx ? ctx->err.c_str() : ""; }
 
+extern "C" int fdgpu_probe_fp64(fdgpu_ctx *ctx, double *gops)
+{
+    if (!ctx || !gops) return FDGPU_EINVAL;
+    FD_CU(ctx, cudaSetDevice(ctx->device));
+    int sms = 0;
+    FD_CU(ctx, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
+    const int blocks = sms * 8, threads = 256, iters = 2048;
+    DevBuf buf;
+    FD_CU(ctx, buf.ensure(sizeof(double) * (size_t)blocks * threads));
+    float ms = 0.f;
+    FD_CU(ctx, fdk_probe_fp64(buf.as<double>(), blocks, threads, iters, &ms, ctx->stream));
+    *gops = (double)blocks * threads * iters * 8 / (ms * 1e-3) / 1e9;   /* FP64 instructions per second */
+    return FDGPU_OK;
+}
+
 extern "C" int fdgpu_velocity_to_slowness(fdgpu_ctx *ctx, const float *v, float *s, long long n, void *stream)
 {
     if (!ctx || (!v && n) || (!s && n) || n < 0) return FDGPU_EINVAL;
@@ -270,15 +287,17 @@ extern "C" int fdgpu_solve_device(fdgpu_ctx *ctx, int n, const fdgpu_station *st
     if (n == 0) return FDGPU_OK;
     FD_CU(ctx, cudaSetDevice(ctx->device));
     cudaStream_t cs = stream ? (cudaStream_t)stream : ctx->stream;
+    if (((uintptr_t)slowness & 3u) != 0) return FDGPU_EINVAL;
     for (int k = 0; k < n; k++) {
         const int c = check_station(st[k]);
         if (c) return c;
-        if (!d_times[k]) return FDGPU_EINVAL;
+        if (!d_times[k] || ((uintptr_t)d_times[k] & 3u) != 0) return FDGPU_EINVAL;
         if (st[k].srctype != 1 && !times_initialised) return FDGPU_EINVAL;
     }
     /* scratch and per-station records */
     std::vector<size_t> off(n + 1, 0);
-    for (int k = 0; k < n; k++) off[k + 1] = off[k] + (size_t)max_face(st[k]) * kScratchPerPoint;
+    for (int k = 0; k < n; k++)
+        off[k + 1] = off[k] + ((((size_t)max_face(st[k]) + 16) * kScratchPerPoint + 255) & ~(size_t)255);
     FD_CU(ctx, ctx->scratch.ensure(off[n]));
     FD_CU(ctx, ctx->stations.ensure(sizeof(fd_station_dev) * n));
     FD_CU(ctx, ctx->stats.ensure(sizeof(fd_station_stats) * n));
@@ -286,6 +305,7 @@ extern "C" int fdgpu_solve_device(fdgpu_ctx *ctx, int n, const fdgpu_station *st
     for (int k = 0; k < n; k++) maxw = std::max(maxw, 2 * st[k].ncube + 1);
     FD_CU(ctx, ctx->trig.ensure(sizeof(double) * 4 * (size_t)maxw * n + 8));
     std::vector<fd_station_dev> hs(n);
+    long long max_pad = 16;
     std::vector<double> trig(4 * (size_t)maxw * n, 0.0);
     for (int k = 0; k < n; k++) {
         const fdgpu_station &s = st[k];
@@ -335,11 +355,14 @@ extern "C" int fdgpu_solve_device(fdgpu_ctx *ctx, int n, const fdgpu_station *st
         d.scr.wl[0] = reinterpret_cast<int *>(base + 20 * m);
         d.scr.wl[1] = reinterpret_cast<int *>(base + 24 * m);
         d.scr.deferred = reinterpret_cast<int *>(base + 28 * m);
+        d.scr.dag = reinterpret_cast<unsigned char *>(base + 32 * m);
+        d.max_face_pad = ((long long)m + 15) & ~15LL;
+        max_pad = std::max(max_pad, d.max_face_pad);
         d.stats = ctx->stats.as<fd_station_stats>() + k;
     }
     FD_CU(ctx, cudaMemcpyAsync(ctx->trig.p, trig.data(), sizeof(double) * trig.size(), cudaMemcpyHostToDevice, cs));
     FD_CU(ctx, cudaMemcpyAsync(ctx->stations.p, hs.data(), sizeof(fd_station_dev) * n, cudaMemcpyHostToDevice, cs));
-    FD_CU(ctx, fdk_launch_solve(ctx->stations.as<fd_station_dev>(), n, cs));
+    FD_CU(ctx, fdk_launch_solve(ctx->stations.as<fd_station_dev>(), n, max_pad, cs));
     std::vector<fd_station_stats> hst(n);
     FD_CU(ctx, cudaMemcpyAsync(hst.data(), ctx->stats.p, sizeof(fd_station_stats) * n, cudaMemcpyDeviceToHost, cs));
     FD_CU(ctx, cudaStreamSynchronize(cs));
@@ -355,6 +378,9 @@ extern "C" int fdgpu_solve_device(fdgpu_ctx *ctx, int n, const fdgpu_station *st
             o.deferred = hst[k].deferred;
             for (int j = 0; j < 5; j++) o.stencils[j] = hst[k].stencils[j];
             for (int j = 0; j < 8; j++) o.restart_wall[j] = hst[k].restart_wall[j];
+            for (int j = 0; j < 6; j++) o.phase_cycles[j] = hst[k].phase_cycles[j];
+            o.t_start_ns = hst[k].t_start_ns;
+            o.t_end_ns = hst[k].t_end_ns;
         }
         if (hst[k].status && rc == FDGPU_OK) rc = FDGPU_ESCHED;
     }
@@ -375,8 +401,12 @@ extern "C" int fdgpu_solve_host(fdgpu_ctx *ctx, int n, const fdgpu_station *st, 
         if (!times[k]) return FDGPU_EINVAL;
     }
     const long long nm = (long long)mnx * mny * mnz;
-    std::vector<size_t> off(n + 1, 0);
-    for (int k = 0; k < n; k++) off[k + 1] = off[k] + (size_t)st[k].nx * st[k].ny * st[k].nz;
+    /* each station's field starts on a 256-byte boundary of the shared field buffer */
+    std::vector<size_t> off(n + 1, 0), len(n);
+    for (int k = 0; k < n; k++) {
+        len[k] = (size_t)st[k].nx * st[k].ny * st[k].nz;
+        off[k + 1] = off[k] + ((len[k] + 63) & ~(size_t)63);
+    }
     FD_CU(ctx, ctx->model.ensure(sizeof(float) * (size_t)nm));
     FD_CU(ctx, ctx->fields.ensure(sizeof(float) * off[n]));
     FD_CU(ctx, cudaMemcpyAsync(ctx->model.p, velocity, sizeof(float) * nm, cudaMemcpyHostToDevice, ctx->stream));
@@ -387,8 +417,8 @@ extern "C" int fdgpu_solve_host(fdgpu_ctx *ctx, int n, const fdgpu_station *st, 
         dt[k] = ctx->fields.as<float>() + off[k];
         if (init_times && init_times[k]) {
             any_init = true;
-            FD_CU(ctx, cudaMemcpyAsync(dt[k], init_times[k], sizeof(float) * (off[k + 1] - off[k]),
-                                       cudaMemcpyHostToDevice, ctx->stream));
+            FD_CU(ctx, cudaMemcpyAsync(dt[k], init_times[k], sizeof(float) * len[k], cudaMemcpyHostToDevice,
+                                       ctx->stream));
         }
     }
     if (any_init) {
@@ -400,8 +430,7 @@ extern "C" int fdgpu_solve_host(fdgpu_ctx *ctx, int n, const fdgpu_station *st, 
                                       any_init ? 1 : 0, stats, ctx->stream);
     if (rc) return rc;
     for (int k = 0; k < n; k++)
-        FD_CU(ctx, cudaMemcpyAsync(times[k], dt[k], sizeof(float) * (off[k + 1] - off[k]), cudaMemcpyDeviceToHost,
-                                   ctx->stream));
+        FD_CU(ctx, cudaMemcpyAsync(times[k], dt[k], sizeof(float) * len[k], cudaMemcpyDeviceToHost, ctx->stream));
     FD_CU(ctx, cudaStreamSynchronize(ctx->stream));
     return FDGPU_OK;
 }

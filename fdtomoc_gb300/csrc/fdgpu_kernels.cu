@@ -27,9 +27,19 @@
 #include <stdint.h>
 
 #include "fdgpu_eval.cuh"
+#include "fdgpu_trials.cuh"
 #include "fdgpu_layout.h"
 
-#define FD_BLOCK 256
+#define FD_BLOCK 512
+
+/* optional per-phase cycle counters (thread 0, between barriers) for profiling builds */
+#ifdef FDGPU_PHASE_TIMERS
+#define FD_TIC(v) long long v = clock64()
+#define FD_TOC(k, v) do { if (threadIdx.x == 0) sh.cyc[k] += clock64() - (v); } while (0)
+#else
+#define FD_TIC(v) do { } while (0)
+#define FD_TOC(k, v) do { } while (0)
+#endif
 #define FD_HEADTEST 1.e-3
 
 namespace fdk {
@@ -115,7 +125,7 @@ struct Shared {
     int ndef;
     unsigned long long exitkey;
     /* current face */
-    int face, layer, ulo, uhi, vlo, vhi, nuf, n;
+    int face, layer, ulo, uhi, vlo, vhi, nuf, n, n_pad;
     long long su, sv, sn, ssu, ssv, ssn;
     int nu, nv;
     int status;
@@ -126,6 +136,7 @@ struct Shared {
     unsigned long long st[5];
     int sweeps;
     int restart_wall[8];
+    long long cyc[6];
 };
 
 /* face frame for a face number known only at run time */
@@ -187,147 +198,493 @@ struct Counters {
     unsigned long long n[5];
 };
 
-/* Evaluate face point i (fill index) of the current face with template face F.  Returns false if
- * the point needs an inherited (t0,t4) it was not given. */
-template <int F>
-__device__ bool eval_point(const fd_station_dev &sd, Shared &sh, int i, bool have_inherit, float it0, float it4,
-                           Counters &cn)
+/* ---------------------------------------------------------------------------------------------- */
+/* trial-major rounds                                                                              */
+
+#define FD_CHUNK 128   /* points per evaluation chunk */
+#define FD_TPP 4       /* threads per point in phase A */
+
+#define FD_DESC_ROW(F)                                                                              \
+    make_desc<F>(0), make_desc<F>(1), make_desc<F>(2), make_desc<F>(3), make_desc<F>(4), make_desc<F>(5), \
+    make_desc<F>(6), make_desc<F>(7), make_desc<F>(8), make_desc<F>(9), make_desc<F>(10), make_desc<F>(11), \
+    make_desc<F>(12), make_desc<F>(13), make_desc<F>(14), make_desc<F>(15), make_desc<F>(16), make_desc<F>(17), \
+    make_desc<F>(18), make_desc<F>(19), make_desc<F>(20), make_desc<F>(21)
+__constant__ TrialDesc c_desc[FDN_NFACE * FDN_NTRIAL] = {FD_DESC_ROW(0), FD_DESC_ROW(1), FD_DESC_ROW(2),
+                                                         FD_DESC_ROW(3), FD_DESC_ROW(4), FD_DESC_ROW(5)};
+
+/* item list regions by kind: 3-D, new-edge, 2-D, new-face, 1-D */
+__device__ __forceinline__ int item_off(int kind)
 {
-    using FT = FaceT<F>;
-    const fd_geo_dev &g = sd.g;
-    PointCtx p;
-    p.u = sh.ulo + i % sh.nuf;
-    p.v = sh.vlo + i / sh.nuf;
-    p.nu = sh.nu;
-    p.nv = sh.nv;
-    p.ulo = sh.ulo; p.uhi = sh.uhi; p.vlo = sh.vlo; p.vhi = sh.vhi;
-    int xyz[3];
-    xyz[FT::AU] = p.u;
-    xyz[FT::AV] = p.v;
-    xyz[FT::AN] = sh.layer;
-    p.z = xyz[2];
-    p.y = xyz[1];
-    const long long nx = g.nx, nxy = (long long)g.nx * g.ny;
-    p.pT = (long long)xyz[2] * nxy + (long long)xyz[1] * nx + xyz[0];
-    const long long pS = (long long)xyz[2] * sd.s_sz + (long long)xyz[1] * sd.s_sy + xyz[0];
+    return (kind == 0 ? 0 : kind == 1 ? 4 : kind == 2 ? 8 : kind == 3 ? 16 : 17) * FD_CHUNK;
+}
+
+__device__ __forceinline__ int kind_of(int K)
+{
+    return K < TK_NE0 ? 0 : K < TK_2D0 ? 1 : K < TK_NF ? 2 : K < TK_1D0 ? 3 : 4;
+}
+
+struct Smem {
+    TrialDesc desc[FDN_NTRIAL];
+    float t[FD_CHUNK][NB_N];
+    float s[FD_CHUNK][NB_N];
+    int idx[FD_CHUNK];               /* fill index of the chunk's point */
+    int z[FD_CHUNK], y[FD_CHUNK];
+    unsigned guardm[FD_CHUNK];       /* trials whose guards pass (first-contact gates excluded) */
+    unsigned evalm[FD_CHUNK];        /* trials whose value was computed in the parallel phases */
+    double res[FD_CHUNK][FDN_NTRIAL];
+    double x2[FD_CHUNK][8];
+    unsigned short items[22 * FD_CHUNK];
+    int cnt[5];
+};
+
+/* dependency state of the current face: one in-degree byte per point (0xFF once done) and one
+ * byte marking which of its 8 neighbours come earlier in sort order; in shared memory after Smem
+ * when the face fits, else in the station's global scratch */
+__device__ __forceinline__ unsigned char *dag_indeg(const fd_station_dev &sd, Smem &sm, bool in_smem)
+{
+    return in_smem ? reinterpret_cast<unsigned char *>(&sm + 1) : sd.scr.dag;
+}
+
+__device__ __forceinline__ void nb_off(int k, int &du, int &dv)
+{
+    /* k = 0..7 over the 3x3 block without its centre, row by row */
+    const int c = k < 4 ? k : k + 1;
+    du = c % 3 - 1;
+    dv = c / 3 - 1;
+}
+
+/* bits of the neighbours of fill index i that lie inside the face rectangle */
+__device__ __forceinline__ unsigned inrect_mask(int iu, int iv, int nuf, int nvf)
+{
+    unsigned m = 0;
 #pragma unroll
-    for (int w = 0; w < 2; w++)
-#pragma unroll
-        for (int dv = -1; dv <= 1; dv++)
-#pragma unroll
-            for (int du = -1; du <= 1; du++) {
-                const int uu = p.u + du, vv = p.v + dv;
-                const bool in = uu >= 0 && uu < p.nu && vv >= 0 && vv < p.nv;
-                float tv = 0.f, sv = 0.f;
-                if (in) {
-                    tv = sd.T[p.pT + du * sh.su + dv * sh.sv + (long long)(w * FT::IN) * sh.sn];
-                    sv = __ldg(&sd.S[pS + du * sh.ssu + dv * sh.ssv + (long long)(w * FT::IN) * sh.ssn]);
-                }
-                p.t[w][dv + 1][du + 1] = tv;
-                p.s[w][dv + 1][du + 1] = sv;
-            }
-    EvalState st;
-    const float told = p.t[0][1][1];
-    st.guess = f2d(told);
-    st.fhead = 0.0;
-    st.t0 = it0;
-    st.t4 = it4;
-    st.writers = 0;
-    st.gate = false;
-    st.have_inherit = have_inherit;
-    st.defer = false;
-    st.n3d = st.nne = st.n2d = st.nnf = st.n1d = 0;
-    run_trials<F, 0>(g, p, st);
-    if (st.defer) return false;
-    cn.n[0] += st.n3d; cn.n[1] += st.nne; cn.n[2] += st.n2d; cn.n[3] += st.nnf; cn.n[4] += st.n1d;
-    if (st.guess < f2d(told)) {
-        sd.T[p.pT] = __double2float_rn(st.guess);
-        if (st.fhead > FD_HEADTEST) atomicAdd(&sh.headw[FT::HW], 1);
+    for (int k = 0; k < 8; k++) {
+        int du, dv;
+        nb_off(k, du, dv);
+        const int ju = iu + du, jv = iv + dv;
+        if (ju >= 0 && ju < nuf && jv >= 0 && jv < nvf) m |= 1u << k;
     }
-    if (st.writers) {
-        sd.scr.rec[i] = make_float2(st.t0, st.t4);
-        atomicMax(&sh.exitkey, sd.scr.key[i]);
-    } else {
-        sd.scr.rec[i] = make_float2(__int_as_float(0x7fc00000), __int_as_float(0x7fc00000));
+    return m;
+}
+
+/* guards without the first-contact gates; t18 = the point's 18-node context */
+template <int F, int K>
+__device__ __forceinline__ bool guard_static(const float *t18, int u, int v, int nu, int nv, int ulo, int uhi,
+                                             int vlo, int vhi)
+{
+    constexpr fdn_trial tr = fd_face_trials[F][K];
+    if constexpr ((tr.need & FDN_NEED_UM) != 0) if (!(u > 0)) return false;
+    if constexpr ((tr.need & FDN_NEED_UP) != 0) if (!(u < nu - 1)) return false;
+    if constexpr ((tr.need & FDN_NEED_VM) != 0) if (!(v > 0)) return false;
+    if constexpr ((tr.need & FDN_NEED_VP) != 0) if (!(v < nv - 1)) return false;
+    if constexpr ((tr.inside & FDN_IN_ULO) != 0) if (!(u > ulo)) return false;
+    if constexpr ((tr.inside & FDN_IN_UHI) != 0) if (!(u < uhi)) return false;
+    if constexpr ((tr.inside & FDN_IN_VLO) != 0) if (!(v > vlo)) return false;
+    if constexpr ((tr.inside & FDN_IN_VHI) != 0) if (!(v < vhi)) return false;
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        if (c < tr.nchk) {
+            const float tv = t18[nb_index(tr.chk[c])];
+            const bool ok = ((tr.chk_nonzero >> c) & 1) ? (tv != 0.0f) : (tv < 1.e9f);
+            if (!ok) return false;
+        }
     }
     return true;
 }
 
-__device__ __forceinline__ bool eval_dispatch(const fd_station_dev &sd, Shared &sh, int i, bool hi, float t0, float t4,
-                                              Counters &cn)
+/* causality floor of trial K: the largest time among the slots its accepted value cannot be below
+ * (2-D: its three own slots; the stale pair is added in the scan) */
+template <int F, int K>
+__device__ __forceinline__ float floor_of(const float *t18)
 {
-    switch (sh.face) {
-    case 0: return eval_point<0>(sd, sh, i, hi, t0, t4, cn);
-    case 1: return eval_point<1>(sd, sh, i, hi, t0, t4, cn);
-    case 2: return eval_point<2>(sd, sh, i, hi, t0, t4, cn);
-    case 3: return eval_point<3>(sd, sh, i, hi, t0, t4, cn);
-    case 4: return eval_point<4>(sd, sh, i, hi, t0, t4, cn);
-    default: return eval_point<5>(sd, sh, i, hi, t0, t4, cn);
+    constexpr fdn_trial tr = fd_face_trials[F][K];
+    constexpr int n = tr.kind == FDN_3D ? 7 : (tr.kind == FDN_NE || tr.kind == FDN_NF) ? 5 : tr.kind == FDN_2D ? 4 : 1;
+    constexpr int i0 = tr.kind == FDN_2D ? 1 : 0;
+    float m = t18[nb_index(tr.t[i0])];
+#pragma unroll
+    for (int i = i0 + 1; i < n; i++) m = fmaxf(m, t18[nb_index(tr.t[i])]);
+    return m;
+}
+
+/* a trial with floor fl cannot lower a running minimum that is at most g (any earlier value of
+ * the running minimum is such a bound): its accepted value is >= fl, and its rejection value
+ * 1e11 is not below g */
+__device__ __forceinline__ bool prunable(float fl, double g) { return f2d(fl) >= g && g <= 1.e11; }
+
+struct Rect {
+    int u, v, nu, nv, ulo, uhi, vlo, vhi;
+};
+
+/* phase A2: thread q of a point handles trials K = q, q+4, ...: guards, pruning, items.  Corner
+ * and edge trials are queued now; new-edge trials only when no corner trial can run (the
+ * first-contact gate is then decided by the initial value); 2-D trials after the corners. */
+template <int F, int K>
+__device__ __forceinline__ void a2_trials(Smem &sm, int slot, const Rect &r, double g0, bool any3d, unsigned &gm,
+                                          unsigned &em)
+{
+    if constexpr (K < FDN_NTRIAL) {
+        constexpr fdn_trial tr = fd_face_trials[F][K];
+        const float *t18 = sm.t[slot];
+        if (guard_static<F, K>(t18, r.u, r.v, r.nu, r.nv, r.ulo, r.uhi, r.vlo, r.vhi)) {
+            gm |= 1u << K;
+            if constexpr (tr.kind == FDN_3D) {
+                if (!prunable(floor_of<F, K>(t18), g0)) em |= 1u << K;
+            } else if constexpr (tr.kind == FDN_1D) {
+                if (!(f2d(floor_of<F, K>(t18)) >= g0)) em |= 1u << K;
+            } else if constexpr (tr.kind == FDN_NE) {
+                if (!any3d && g0 > 1.0e9 && !prunable(floor_of<F, K>(t18), g0)) em |= 1u << K;
+            }
+        }
+        a2_trials<F, K + FD_TPP>(sm, slot, r, g0, any3d, gm, em);
     }
 }
 
-/* mark point i done and release its later in-face neighbours into list `out` */
-__device__ __forceinline__ void release(const fd_station_dev &sd, Shared &sh, int i, int out)
+template <int F>
+__device__ __forceinline__ bool any_corner(const float *t18, const Rect &r)
 {
-    const unsigned long long ki = sd.scr.key[i];
-    sd.scr.indeg[i] = -1;
-    const int iu = i % sh.nuf, iv = i / sh.nuf;
-    const int nvf = sh.n / sh.nuf;
-#pragma unroll
-    for (int dv = -1; dv <= 1; dv++)
-#pragma unroll
-        for (int du = -1; du <= 1; du++) {
-            if (du == 0 && dv == 0) continue;
-            const int ju = iu + du, jv = iv + dv;
-            if (ju < 0 || ju >= sh.nuf || jv < 0 || jv >= nvf) continue;
-            const int j = jv * sh.nuf + ju;
-            if (sd.scr.key[j] > ki) {
-                if (atomicSub(&sd.scr.indeg[j], 1) == 1) {
-                    const int pos = atomicAdd(&sh.cnt[out], 1);
-                    sd.scr.wl[out][pos] = j;
-                }
-            }
+    return guard_static<F, 0>(t18, r.u, r.v, r.nu, r.nv, r.ulo, r.uhi, r.vlo, r.vhi)
+           || guard_static<F, 1>(t18, r.u, r.v, r.nu, r.nv, r.ulo, r.uhi, r.vlo, r.vhi)
+           || guard_static<F, 2>(t18, r.u, r.v, r.nu, r.nv, r.ulo, r.uhi, r.vlo, r.vhi)
+           || guard_static<F, 3>(t18, r.u, r.v, r.nu, r.nv, r.ulo, r.uhi, r.vlo, r.vhi);
+}
+
+__device__ __forceinline__ Rect rect_of(const Shared &sh, int i)
+{
+    Rect r;
+    r.u = sh.ulo + i % sh.nuf;
+    r.v = sh.vlo + i / sh.nuf;
+    r.nu = sh.nu; r.nv = sh.nv;
+    r.ulo = sh.ulo; r.uhi = sh.uhi; r.vlo = sh.vlo; r.vhi = sh.vhi;
+    return r;
+}
+
+template <int F>
+__device__ void phase_a2(Smem &sm, const Shared &sh, int slot, int q)
+{
+    const int i = sm.idx[slot];
+    const Rect r = rect_of(sh, i);
+    const float *t18 = sm.t[slot];
+    const double g0 = f2d(t18[NB_POINT]);
+    const bool any3d = any_corner<F>(t18, r);
+    unsigned gm = 0, em = 0;
+    switch (q) {
+    case 0: a2_trials<F, 0>(sm, slot, r, g0, any3d, gm, em); break;
+    case 1: a2_trials<F, 1>(sm, slot, r, g0, any3d, gm, em); break;
+    case 2: a2_trials<F, 2>(sm, slot, r, g0, any3d, gm, em); break;
+    default: a2_trials<F, 3>(sm, slot, r, g0, any3d, gm, em); break;
+    }
+    if (gm) atomicOr(&sm.guardm[slot], gm);
+    if (em) atomicOr(&sm.evalm[slot], em);
+    unsigned m = em;
+    while (m) {
+        const int K = __ffs(m) - 1;
+        m &= m - 1;
+        const int kind = kind_of(K);
+        sm.items[item_off(kind) + atomicAdd(&sm.cnt[kind], 1)] = (unsigned short)((slot << 5) | K);
+    }
+}
+
+/* phase G: replay the corner and new-edge trials (all writers of the stencil state come before
+ * the 2-D block) to get the running minimum entering the 2-D block — an upper bound for every
+ * 2-D trial's turn — and the stale (t0,t4) those trials test against; queue the 2-D trials that
+ * can still lower the minimum.  Thread q takes 2-D trials 8+q and 12+q. */
+__device__ void phase_g(Smem &sm, int slot, int q, float it0, float it4)
+{
+    const float *t18 = sm.t[slot];
+    const unsigned gm = sm.guardm[slot], em = sm.evalm[slot];
+    double g1 = f2d(t18[NB_POINT]);
+    float s0 = it0, s4 = it4;
+    for (int K = 0; K < TK_NE0; K++) {
+        if (!((gm >> K) & 1u)) continue;
+        s0 = t18[sm.desc[K].slot[0]];
+        s4 = t18[sm.desc[K].slot[4]];
+        if ((em >> K) & 1u) {
+            const double v = sm.res[slot][K];
+            if (lt(v, g1)) g1 = v;
         }
+    }
+    const bool gate = lt(1.0e9, g1);
+    for (int K = TK_NE0; K < TK_2D0; K++) {
+        if (!gate || !((gm >> K) & 1u)) continue;
+        s0 = t18[sm.desc[K].slot[0]];
+        s4 = t18[sm.desc[K].slot[4]];
+        if ((em >> K) & 1u) {
+            const double v = sm.res[slot][K];
+            if (lt(v, g1)) g1 = v;
+        }
+    }
+    unsigned add = 0;
+    for (int K = TK_2D0 + q; K < TK_NF; K += FD_TPP) {
+        if (!((gm >> K) & 1u)) continue;
+        const TrialDesc &d = sm.desc[K];
+        const float fl = fmaxf(fmaxf(fmaxf(t18[d.slot[1]], t18[d.slot[2]]), fmaxf(t18[d.slot[3]], s0)), s4);
+        if (prunable(fl, g1)) continue;
+        add |= 1u << K;
+        sm.items[item_off(2) + atomicAdd(&sm.cnt[2], 1)] = (unsigned short)((slot << 5) | K);
+    }
+    if (add) atomicOr(&sm.evalm[slot], add);
+}
+
+/* evaluate queued items of kinds [k0, k1] with all threads */
+__device__ void run_items(const fd_station_dev &sd, Smem &sm, int k0, int k1, Counters &cn)
+{
+    int start[6];
+    start[0] = 0;
+    for (int k = 0; k < 5; k++) start[k + 1] = start[k] + ((k >= k0 && k <= k1) ? sm.cnt[k] : 0);
+    const int total = start[5];
+    for (int j = threadIdx.x; j < total; j += blockDim.x) {
+        int kind = 0;
+        while (j >= start[kind + 1]) kind++;
+        const unsigned it = sm.items[item_off(kind) + (j - start[kind])];
+        const int slot = (int)(it >> 5), K = (int)(it & 31);
+        const TrialDesc &d = sm.desc[K];
+        const int z = sm.z[slot], y = sm.y[slot];
+        const float *t18 = sm.t[slot], *s18 = sm.s[slot];
+        switch (kind) {
+        case 0: sm.res[slot][K] = eval_3d(d, t18, s18, sd.g, z, y); break;
+        case 1: sm.res[slot][K] = eval_ne(d, t18, s18, sd.g, z, y); break;
+        case 2: {
+            double x1, x2;
+            eval_2d(d, t18, s18, sd.g, z, y, x1, x2);
+            sm.res[slot][K] = x1;
+            sm.x2[slot][K - TK_2D0] = x2;
+            break;
+        }
+        case 3: sm.res[slot][K] = eval_nf(d, t18, s18, sd.g, z, y); break;
+        default: sm.res[slot][K] = eval_1d(d, t18, s18, sd.g, z, y); break;
+        }
+        cn.n[kind]++;
+    }
+}
+
+/* Phase C for one point: the reference's sequential minimum over the 22 trials, from the values
+ * computed in the parallel phases (new-edge and new-face values that were not precomputed are
+ * evaluated here — they are needed only at first contact), then the commit
+ * (src/sphfd.c:1756-1760), the point's stencil-state record and the release of its later
+ * neighbours into list `out`.  Returns false if the point must wait for an inherited state. */
+__device__ bool phase_c(const fd_station_dev &sd, Shared &sh, Smem &sm, int slot, bool have_inherit, float it0,
+                        float it4, int out, unsigned char *dag, Counters &cn)
+{
+    const int i = sm.idx[slot];
+    const float *t18 = sm.t[slot], *s18 = sm.s[slot];
+    const unsigned gm = sm.guardm[slot], em = sm.evalm[slot];
+    const double told = f2d(t18[NB_POINT]);
+    /* a 2-D trial before any corner / new-edge call would read the previous point's t0,t4 */
+    if (!have_inherit && (gm & 0xFu) == 0 && !((gm & 0xF0u) && told > 1.0e9) && (gm & 0xFF00u)) return false;
+    const int z = sm.z[slot], y = sm.y[slot];
+    double guess = told;
+    float st0 = it0, st4 = it4;
+    int writers = 0;
+    bool gate = false;
+    int lastK = -1;
+    double last_gb = 0.0, last_v = 0.0;
+#pragma unroll 1
+    for (int K = 0; K < FDN_NTRIAL; K++) {
+        /* the first-contact tests are made on entry to their blocks (src/sphfd.c:1375, :1698) */
+        if (K == TK_NE0 || K == TK_NF) gate = lt(1.0e9, guess);
+        if (!((gm >> K) & 1u)) continue;
+        const TrialDesc &d = sm.desc[K];
+        const bool ev = (em >> K) & 1u;
+        double v;
+        if (K < TK_2D0 || K == TK_NF) {
+            /* corner, new-edge, new-face: writers of the stencil state */
+            if (K >= TK_NE0 && !gate) continue;
+            st0 = t18[d.slot[0]];
+            st4 = t18[d.slot[4]];
+            writers++;
+            if (ev) {
+                v = sm.res[slot][K];
+            } else if (K >= TK_NE0) {
+                /* new-edge / new-face value not precomputed: evaluate unless it cannot improve */
+                float fl = t18[d.slot[0]];
+                for (int k = 1; k < 5; k++) fl = fmaxf(fl, t18[d.slot[k]]);
+                if (prunable(fl, guess)) continue;
+                v = (K == TK_NF) ? eval_nf(d, t18, s18, sd.g, z, y) : eval_ne(d, t18, s18, sd.g, z, y);
+                cn.n[K == TK_NF ? 3 : 1]++;
+            } else {
+                continue;
+            }
+        } else if (K < TK_NF) {
+            /* 2-D: the causality floor includes the stale t0,t4 */
+            if (!ev) continue;
+            const float fl = fmaxf(fmaxf(fmaxf(t18[d.slot[1]], t18[d.slot[2]]), fmaxf(t18[d.slot[3]], st0)), st4);
+            const double x1 = sm.res[slot][K], x2 = sm.x2[slot][K - TK_2D0];
+            if (x1 != x1) {
+                v = 1.e11;
+            } else {
+                const double f = f2d(fl);
+                const bool bad1 = lt(x1, f), bad2 = lt(x2, f);
+                v = bad1 ? (bad2 ? 1.e11 : x2) : (bad2 ? x1 : (lt(x2, x1) ? x2 : x1));
+            }
+        } else {
+            if (!ev) continue;
+            v = sm.res[slot][K];
+        }
+        if (lt(v, guess)) {
+            if (d.head) { lastK = K; last_gb = guess; last_v = v; }
+            guess = v;
+        }
+    }
+    if (lt(guess, told)) {
+        const fdn_frame fr = frame_of(sh.face);
+        int xyz[3];
+        xyz[fr.axis_u] = sh.ulo + i % sh.nuf;
+        xyz[fr.axis_v] = sh.vlo + i / sh.nuf;
+        xyz[fr.axis_n] = sh.layer;
+        const long long pT = ((long long)xyz[2] * sd.g.ny + xyz[1]) * sd.g.nx + xyz[0];
+        sd.T[pT] = __double2float_rn(guess);
+        if (lastK >= 0) {
+            /* only the last head trial that lowered the minimum sets the measure that is tested */
+            const double fhead = (last_gb - last_v) / head_den(sm.desc[lastK], s18, sd.g, z, y);
+            if (fhead > FD_HEADTEST) atomicAdd(&sh.headw[fr.headw], 1);
+        }
+    }
+    if (writers) {
+        sd.scr.rec[i] = make_float2(st0, st4);
+        atomicMax(&sh.exitkey, sd.scr.key[i]);
+    } else {
+        sd.scr.rec[i] = make_float2(__int_as_float(0x7fc00000), __int_as_float(0x7fc00000));
+    }
+    /* done; release the later in-face neighbours */
+    const int nvf = sh.n / sh.nuf, iu = i % sh.nuf, iv = i / sh.nuf;
+    unsigned char *emask = dag + sh.n_pad;
+    unsigned later = inrect_mask(iu, iv, sh.nuf, nvf) & ~(unsigned)emask[i];
+    atomicOr(reinterpret_cast<unsigned *>(dag) + (i >> 2), 0xFFu << ((i & 3) * 8));
+    while (later) {
+        const int k = __ffs(later) - 1;
+        later &= later - 1;
+        int du, dv;
+        nb_off(k, du, dv);
+        const int j = (iv + dv) * sh.nuf + iu + du;
+        const unsigned sh8 = (j & 3) * 8;
+        const unsigned old = atomicSub(reinterpret_cast<unsigned *>(dag) + (j >> 2), 1u << sh8);
+        if (((old >> sh8) & 0xFFu) == 1u) sd.scr.wl[out][atomicAdd(&sh.cnt[out], 1)] = j;
+    }
+    return true;
+}
+
+__device__ __forceinline__ void phase_a2_dispatch(Smem &sm, const Shared &sh, int slot, int q)
+{
+    switch (sh.face) {
+    case 0: phase_a2<0>(sm, sh, slot, q); break;
+    case 1: phase_a2<1>(sm, sh, slot, q); break;
+    case 2: phase_a2<2>(sm, sh, slot, q); break;
+    case 3: phase_a2<3>(sm, sh, slot, q); break;
+    case 4: phase_a2<4>(sm, sh, slot, q); break;
+    default: phase_a2<5>(sm, sh, slot, q); break;
+    }
+}
+
+/* Evaluate points list[0..m) (m <= FD_CHUNK).  All threads call this. */
+__device__ void run_chunk(const fd_station_dev &sd, Shared &sh, Smem &sm, const int *list, int m, bool have_inherit,
+                          float it0, float it4, int out, unsigned char *dag, Counters &cn)
+{
+    const int tid = threadIdx.x;
+    if (tid < 5) sm.cnt[tid] = 0;
+    FD_TIC(ta);
+    /* A1: the 18-node context of each point, FD_TPP threads per point */
+    const fdn_frame fr = frame_of(sh.face);
+    for (int r = tid; r < m * FD_TPP; r += blockDim.x) {
+        const int slot = r / FD_TPP, q = r % FD_TPP;
+        const int i = list[slot];
+        const int u = sh.ulo + i % sh.nuf, v = sh.vlo + i / sh.nuf;
+        int xyz[3];
+        xyz[fr.axis_u] = u;
+        xyz[fr.axis_v] = v;
+        xyz[fr.axis_n] = sh.layer;
+        const long long pT = ((long long)xyz[2] * sd.g.ny + xyz[1]) * sd.g.nx + xyz[0];
+        const long long pS = (long long)xyz[2] * sd.s_sz + (long long)xyz[1] * sd.s_sy + xyz[0];
+        if (q == 0) {
+            sm.idx[slot] = i;
+            sm.z[slot] = xyz[2];
+            sm.y[slot] = xyz[1];
+            sm.guardm[slot] = 0;
+            sm.evalm[slot] = 0;
+        }
+        for (int nb = q; nb < NB_N; nb += FD_TPP) {
+            const int w = nb / 9, dv = (nb / 3) % 3 - 1, du = nb % 3 - 1;
+            const int uu = u + du, vv = v + dv;
+            float tv = 0.f, svv = 0.f;
+            if (uu >= 0 && uu < sh.nu && vv >= 0 && vv < sh.nv) {
+                const long long off_n = (long long)(w * fr.inner);
+                tv = sd.T[pT + du * sh.su + dv * sh.sv + off_n * sh.sn];
+                svv = __ldg(&sd.S[pS + du * sh.ssu + dv * sh.ssv + off_n * sh.ssn]);
+            }
+            sm.t[slot][nb] = tv;
+            sm.s[slot][nb] = svv;
+        }
+    }
+    __syncthreads();
+    /* A2: guards, pruning, corner / edge / first-contact items */
+    for (int r = tid; r < m * FD_TPP; r += blockDim.x) phase_a2_dispatch(sm, sh, r / FD_TPP, r % FD_TPP);
+    __syncthreads();
+    FD_TOC(1, ta);
+    FD_TIC(tb);
+    run_items(sd, sm, 0, 4, cn);   /* corner, new-edge, 1-D (2-D not queued yet, new-face never) */
+    __syncthreads();
+    if (tid < 5) sm.cnt[tid] = 0;
+    __syncthreads();
+    for (int r = tid; r < m * FD_TPP; r += blockDim.x) phase_g(sm, r / FD_TPP, r % FD_TPP, it0, it4);
+    __syncthreads();
+    run_items(sd, sm, 2, 2, cn);
+    __syncthreads();
+    FD_TOC(2, tb);
+    FD_TIC(tc);
+    if (tid < m) {
+        if (!phase_c(sd, sh, sm, tid, have_inherit, it0, it4, out, dag, cn))
+            sd.scr.deferred[atomicAdd(&sh.ndef, 1)] = list[tid];
+    }
+    __syncthreads();
+    FD_TOC(3, tc);
 }
 
 /* Walk the current face (parameters in sh) in dependency order. */
-__device__ void face_walk(const fd_station_dev &sd, Shared &sh, Counters &cn)
+__device__ void face_walk(const fd_station_dev &sd, Shared &sh, Smem &sm, bool dag_in_smem, Counters &cn)
 {
     const int n = sh.n, nuf = sh.nuf, nvf = n / nuf;
     const int tid = threadIdx.x;
     const float *T = sd.T;
-    /* keys: time of the inner-layer neighbour, then fill index */
     const fdn_frame fr = frame_of(sh.face);
-    const int IN = fr.inner;
-    for (int i = tid; i < n; i += FD_BLOCK) {
-        const int u = sh.ulo + i % nuf, v = sh.vlo + i / nuf;
+    unsigned char *dag = dag_indeg(sd, sm, dag_in_smem);
+    unsigned char *emask = dag + sh.n_pad;
+    FD_TIC(t0);
+    /* trial descriptors of this face */
+    for (int k = tid; k < FDN_NTRIAL; k += blockDim.x) sm.desc[k] = c_desc[sh.face * FDN_NTRIAL + k];
+    /* keys: time of the inner-layer neighbour, then fill index */
+    for (int i = tid; i < n; i += blockDim.x) {
         int xyz[3];
-        xyz[fr.axis_u] = u;
-        xyz[fr.axis_v] = v;
-        xyz[fr.axis_n] = sh.layer + IN;
-        const float tin = T[(long long)xyz[2] * sd.g.nx * sd.g.ny + (long long)xyz[1] * sd.g.nx + xyz[0]];
+        xyz[fr.axis_u] = sh.ulo + i % nuf;
+        xyz[fr.axis_v] = sh.vlo + i / nuf;
+        xyz[fr.axis_n] = sh.layer + fr.inner;
+        const float tin = T[((long long)xyz[2] * sd.g.ny + xyz[1]) * sd.g.nx + xyz[0]];
         sd.scr.key[i] = ((unsigned long long)okey32(tin) << 32) | (unsigned)i;
     }
     if (tid == 0) { sh.cnt[0] = 0; sh.cnt[1] = 0; sh.ndef = 0; sh.exitkey = 0ull; }
     __syncthreads();
-    for (int i = tid; i < n; i += FD_BLOCK) {
+    /* earlier-neighbour masks and in-degrees */
+    for (int i = tid; i < n; i += blockDim.x) {
         const unsigned long long ki = sd.scr.key[i];
         const int iu = i % nuf, iv = i / nuf;
-        int c = 0;
-        for (int dv = -1; dv <= 1; dv++)
-            for (int du = -1; du <= 1; du++) {
-                if (du == 0 && dv == 0) continue;
-                const int ju = iu + du, jv = iv + dv;
-                if (ju < 0 || ju >= nuf || jv < 0 || jv >= nvf) continue;
-                c += sd.scr.key[jv * nuf + ju] < ki;
-            }
-        sd.scr.indeg[i] = c;
-        if (c == 0) sd.scr.wl[0][atomicAdd(&sh.cnt[0], 1)] = i;
+        unsigned em = 0;
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            int du, dv;
+            nb_off(k, du, dv);
+            const int ju = iu + du, jv = iv + dv;
+            if (ju < 0 || ju >= nuf || jv < 0 || jv >= nvf) continue;
+            if (sd.scr.key[jv * nuf + ju] < ki) em |= 1u << k;
+        }
+        emask[i] = (unsigned char)em;
+        dag[i] = (unsigned char)__popc(em);
+        if (em == 0) sd.scr.wl[0][atomicAdd(&sh.cnt[0], 1)] = i;
     }
+    __syncthreads();
+    FD_TOC(0, t0);
     int cur = 0;
     long long rounds = 0;
     const long long max_rounds = 2ll * n + 8;
     for (;;) {
+        FD_TIC(tr);
         __syncthreads();
         const int ncur = sh.cnt[cur];
         const int ndef = sh.ndef;
@@ -339,44 +696,43 @@ __device__ void face_walk(const fd_station_dev &sd, Shared &sh, Counters &cn)
             if (ndef == 0) break;
             /* the deferred point with the smallest key: every point below it is done */
             unsigned long long lm = ~0ull;
-            for (int j = tid; j < ndef; j += FD_BLOCK) {
+            for (int j = tid; j < ndef; j += blockDim.x) {
                 const unsigned long long k = sd.scr.key[sd.scr.deferred[j]];
                 lm = k < lm ? k : lm;
             }
             const unsigned long long dmin = block_min_u64(lm, sh);
             /* the last writer before it in sort order */
             unsigned long long lw = 0ull;
-            for (int i = tid; i < n; i += FD_BLOCK) {
+            for (int i = tid; i < n; i += blockDim.x) {
                 const unsigned long long k = sd.scr.key[i];
-                if (k < dmin && sd.scr.indeg[i] < 0 && !isnan(sd.scr.rec[i].x)) lw = k > lw ? k : lw;
+                if (k < dmin && dag[i] == 0xFFu && !isnan(sd.scr.rec[i].x)) lw = k > lw ? k : lw;
             }
             const unsigned long long wkey = block_max_u64(lw, sh);
+            const int d = (int)(dmin & 0xffffffffu);
+            float t0 = sh.carry_t0, t4 = sh.carry_t4;
+            if (wkey) {
+                const float2 r = sd.scr.rec[(int)(wkey & 0xffffffffu)];
+                t0 = r.x;
+                t4 = r.y;
+            }
             if (tid == 0) {
-                const int d = (int)(dmin & 0xffffffffu);
-                float t0 = sh.carry_t0, t4 = sh.carry_t4;
-                if (wkey) {
-                    const float2 r = sd.scr.rec[(int)(wkey & 0xffffffffu)];
-                    t0 = r.x;
-                    t4 = r.y;
-                }
-                eval_dispatch(sd, sh, d, true, t0, t4, cn);
-                release(sd, sh, d, cur);
-                for (int j = 0; j < sh.ndef; j++)
-                    if (sd.scr.deferred[j] == d) { sd.scr.deferred[j] = sd.scr.deferred[sh.ndef - 1]; break; }
-                sh.ndef--;
+                for (int j = 0; j < ndef; j++)
+                    if (sd.scr.deferred[j] == d) { sd.scr.deferred[j] = sd.scr.deferred[ndef - 1]; break; }
+                sh.ndef = ndef - 1;
                 sh.deferred++;
             }
+            __syncthreads();
+            const int one[1] = {d};
+            run_chunk(sd, sh, sm, one, 1, true, t0, t4, cur, dag, cn);
+            FD_TOC(5, tr);
             continue;
         }
         if (tid == 0) { sh.cnt[cur ^ 1] = 0; sh.rounds++; }
         __syncthreads();
-        for (int j = tid; j < ncur; j += FD_BLOCK) {
-            const int i = sd.scr.wl[cur][j];
-            if (eval_dispatch(sd, sh, i, false, 0.f, 0.f, cn)) {
-                release(sd, sh, i, cur ^ 1);
-            } else {
-                sd.scr.deferred[atomicAdd(&sh.ndef, 1)] = i;
-            }
+        FD_TOC(4, tr);
+        for (int c0 = 0; c0 < ncur; c0 += FD_CHUNK) {
+            const int m = ncur - c0 < FD_CHUNK ? ncur - c0 : FD_CHUNK;
+            run_chunk(sd, sh, sm, sd.scr.wl[cur] + c0, m, false, 0.f, 0.f, cur ^ 1, dag, cn);
         }
         cur ^= 1;
     }
@@ -398,10 +754,15 @@ __device__ void face_walk(const fd_station_dev &sd, Shared &sh, Counters &cn)
 __device__ void init_field(const fd_station_dev &sd)
 {
     const long long nxyz = (long long)sd.g.nx * sd.g.ny * sd.g.nz;
-    float4 *T4 = reinterpret_cast<float4 *>(sd.T);
     const float u = 1.0e10f;
-    for (long long i = threadIdx.x; i < nxyz / 4; i += blockDim.x) T4[i] = make_float4(u, u, u, u);
-    for (long long i = (nxyz / 4) * 4 + threadIdx.x; i < nxyz; i += blockDim.x) sd.T[i] = u;
+    /* T may start anywhere a float can: scalar head up to a 16-byte boundary, float4 body, scalar tail */
+    const long long head = (long long)(((16u - ((unsigned)(uintptr_t)sd.T & 15u)) & 15u) / 4u);
+    const long long h = head < nxyz ? head : nxyz;
+    for (long long i = threadIdx.x; i < h; i += blockDim.x) sd.T[i] = u;
+    float4 *T4 = reinterpret_cast<float4 *>(sd.T + h);
+    const long long nv4 = (nxyz - h) / 4;
+    for (long long i = threadIdx.x; i < nv4; i += blockDim.x) T4[i] = make_float4(u, u, u, u);
+    for (long long i = h + nv4 * 4 + threadIdx.x; i < nxyz; i += blockDim.x) sd.T[i] = u;
     __syncthreads();
     const int nc = sd.ncube, w = 2 * nc + 1;
     const long long nx = sd.g.nx, nxy = (long long)sd.g.nx * sd.g.ny;
@@ -426,12 +787,18 @@ __device__ void init_field(const fd_station_dev &sd)
 /* ---------------------------------------------------------------------------------------------- */
 /* the sweep loop (src/sphfd.c:1008-5678)                                                          */
 
-__global__ void __launch_bounds__(FD_BLOCK) fd_solve(const fd_station_dev *stations, int nst)
+__global__ void __launch_bounds__(FD_BLOCK, 1) fd_solve(const fd_station_dev *stations, int nst, int dag_smem_bytes)
 {
     __shared__ Shared sh;
+    extern __shared__ __align__(16) unsigned char fd_dyn_smem[];
+    Smem &sm = *reinterpret_cast<Smem *>(fd_dyn_smem);
     if ((int)blockIdx.x >= nst) return;
     const fd_station_dev &sd = stations[blockIdx.x];
     const int tid = threadIdx.x;
+    unsigned long long t_start = 0;
+    if (tid == 0) asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t_start));
+    /* the dependency bytes of the station's largest face go to shared memory when they fit */
+    const bool dag_in_smem = 2ll * sd.max_face_pad <= dag_smem_bytes;
     if (sd.init_mode == 0) init_field(sd);
     if (tid == 0) {
         for (int f = 0; f < 6; f++) { sh.wall[f] = sd.wall[f]; sh.dflag[f] = sd.dflag[f]; }
@@ -446,6 +813,7 @@ __global__ void __launch_bounds__(FD_BLOCK) fd_solve(const fd_station_dev *stati
         for (int k = 0; k < 5; k++) sh.st[k] = 0;
         sh.sweeps = 0;
         for (int k = 0; k < 8; k++) sh.restart_wall[k] = 0;
+        for (int k = 0; k < 6; k++) sh.cyc[k] = 0;
     }
     __syncthreads();
     Counters cn;
@@ -486,9 +854,10 @@ __global__ void __launch_bounds__(FD_BLOCK) fd_solve(const fd_station_dev *stati
                         sh.nuf = sh.uhi - sh.ulo + 1;
                         const int nvf = sh.vhi - sh.vlo + 1;
                         sh.n = (sh.nuf > 0 && nvf > 0) ? sh.nuf * nvf : 0;
+                        sh.n_pad = (sh.n + 15) & ~15;
                     }
                     __syncthreads();
-                    if (sh.n > 0) face_walk(sd, sh, cn);
+                    if (sh.n > 0) face_walk(sd, sh, sm, dag_in_smem, cn);
                     __syncthreads();
                     if (tid == 0) {
                         /* move the wall outward (e.g. src/sphfd.c:1762-1764) */
@@ -548,6 +917,11 @@ __global__ void __launch_bounds__(FD_BLOCK) fd_solve(const fd_station_dev *stati
         o->deferred = sh.deferred;
         for (int k = 0; k < 5; k++) o->stencils[k] = (int64_t)sh.st[k];
         for (int k = 0; k < 8; k++) o->restart_wall[k] = sh.restart_wall[k];
+        for (int k = 0; k < 6; k++) o->phase_cycles[k] = sh.cyc[k];
+        unsigned long long t_end;
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t_end));
+        o->t_start_ns = (int64_t)t_start;
+        o->t_end_ns = (int64_t)t_end;
     }
 }
 
@@ -562,10 +936,20 @@ extern "C" cudaError_t fdk_launch_geo_build(int nx, int ny, int nz, double h, do
     return cudaGetLastError();
 }
 
-extern "C" cudaError_t fdk_launch_solve(const fd_station_dev *stations, int nst, cudaStream_t stream)
+extern "C" cudaError_t fdk_launch_solve(const fd_station_dev *stations, int nst, long long max_face_pad,
+                                        cudaStream_t stream)
 {
     if (nst <= 0) return cudaSuccess;
-    fdk::fd_solve<<<nst, FD_BLOCK, 0, stream>>>(stations, nst);
+    /* dynamic shared memory: the evaluation chunk, plus the face's dependency bytes if they fit */
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    const long long base = (long long)sizeof(fdk::Smem);
+    const long long want = base + 2 * max_face_pad;
+    const long long bytes = want <= optin - 1024 ? want : base;
+    const cudaError_t e = cudaFuncSetAttribute(fdk::fd_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e != cudaSuccess) return e;
+    fdk::fd_solve<<<nst, FD_BLOCK, (size_t)bytes, stream>>>(stations, nst, (int)(bytes - base));
     return cudaGetLastError();
 }
 
@@ -583,4 +967,33 @@ extern "C" cudaError_t fdk_launch_v2s(const float *v, float *s, long long n, cud
     if (blocks > 152 * 16) blocks = 152 * 16;
     fd_v2s<<<(int)blocks, 256, 0, stream>>>(v, s, n);
     return cudaGetLastError();
+}
+
+/* FP64 pipe rate probe: 8 independent fused multiply-add chains per thread, all SMs */
+__global__ void fd_fp64_probe(double *out, int iters)
+{
+    double a0 = threadIdx.x * 1e-9 + 1.0, a1 = a0 + 1e-3, a2 = a0 + 2e-3, a3 = a0 + 3e-3;
+    double a4 = a0 + 4e-3, a5 = a0 + 5e-3, a6 = a0 + 6e-3, a7 = a0 + 7e-3;
+    const double m = 1.0000001, c = 1e-12;
+    for (int i = 0; i < iters; i++) {
+        a0 = __fma_rn(a0, m, c); a1 = __fma_rn(a1, m, c); a2 = __fma_rn(a2, m, c); a3 = __fma_rn(a3, m, c);
+        a4 = __fma_rn(a4, m, c); a5 = __fma_rn(a5, m, c); a6 = __fma_rn(a6, m, c); a7 = __fma_rn(a7, m, c);
+    }
+    out[(long long)blockIdx.x * blockDim.x + threadIdx.x] = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+}
+
+extern "C" cudaError_t fdk_probe_fp64(double *scratch, int blocks, int threads, int iters, float *ms, cudaStream_t s)
+{
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    fd_fp64_probe<<<blocks, threads, 0, s>>>(scratch, iters);
+    cudaEventRecord(e0, s);
+    fd_fp64_probe<<<blocks, threads, 0, s>>>(scratch, iters);
+    cudaEventRecord(e1, s);
+    cudaError_t e = cudaEventSynchronize(e1);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return e == cudaSuccess ? cudaGetLastError() : e;
 }

@@ -68,6 +68,9 @@ typedef struct {
     int64_t deferred;        /* points that waited for an earlier point's (t0,t4) */
     int64_t stencils[5];     /* stencil evaluations by kind (3d ne 2d nf 1d), after pruning */
     int32_t restart_wall[8]; /* how often each wall (1..6) was chosen for a restart */
+    int64_t phase_cycles[6]; /* with FDGPU_PHASE_TIMERS: SM cycles in face set-up, phases A, B, C,
+                                round bookkeeping, deferred resolution (zero otherwise) */
+    int64_t t_start_ns, t_end_ns; /* GPU global timer when the station's solve began and ended */
 } fd_station_stats;
 
 /* Face-walk scratch of one station, sized for its largest face. */
@@ -77,6 +80,8 @@ typedef struct {
     int *wl[2];                /* ready lists */
     float2 *rec;               /* (t0,t4) the point left in the stencil state; NaN if no writer */
     int *deferred;             /* points waiting for an earlier point's (t0,t4) */
+    unsigned char *dag;        /* in-degree and earlier-neighbour bytes (2 per point) when they do
+                                  not fit in shared memory */
 } fd_scratch_dev;
 
 typedef struct {
@@ -94,6 +99,7 @@ typedef struct {
     double src_xyz[3];         /* Cartesian source point (x1p, y1p, z1p of src/sphfd.c:727-729) */
     const double *box_trig;    /* per box column: cos q, sin q (y) then cos f, sin f (x) */
     fd_scratch_dev scr;
+    long long max_face_pad;    /* largest face, rounded up to 16 points */
     fd_station_stats *stats;
 } fd_station_dev;
 

@@ -12,7 +12,7 @@ import os
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libfdgpu.so")
+LIB_PATH = os.environ.get("FDGPU_LIB") or os.path.join(HERE, "libfdgpu.so")
 
 FDGPU_OK = 0
 ERRORS = {-1: "EINVAL", -2: "ENOMEM", -3: "ECUDA", -4: "EIO", -5: "EPAR", -6: "ESOURCE", -7: "ESCHED", -8: "ENODEV"}
@@ -37,12 +37,14 @@ class Station(C.Structure):
 class Stats(C.Structure):
     _fields_ = [("status", C.c_int32), ("sweeps", C.c_int32), ("node_updates", C.c_int64), ("faces", C.c_int64),
                 ("rounds", C.c_int64), ("deferred", C.c_int64), ("stencils", C.c_int64 * 5),
-                ("restart_wall", C.c_int32 * 8)]
+                ("restart_wall", C.c_int32 * 8), ("phase_cycles", C.c_int64 * 6), ("t_start_ns", C.c_int64),
+                ("t_end_ns", C.c_int64)]
 
     def as_dict(self):
         return dict(status=self.status, sweeps=self.sweeps, node_updates=self.node_updates, faces=self.faces,
                     rounds=self.rounds, deferred=self.deferred, stencils=list(self.stencils),
-                    restart_wall=list(self.restart_wall))
+                    restart_wall=list(self.restart_wall), phase_cycles=list(self.phase_cycles),
+                    t_start_ns=self.t_start_ns, t_end_ns=self.t_end_ns)
 
 
 class FdgpuError(RuntimeError):
@@ -73,6 +75,7 @@ def load() -> C.CDLL:
                                          C.POINTER(C.POINTER(C.c_float)), C.POINTER(Stats)]
         lib.fdgpu_solve_device.argtypes = [P, C.c_int, C.POINTER(Station), C.c_void_p, C.c_longlong, C.c_longlong,
                                            C.POINTER(C.c_void_p), C.c_int, C.POINTER(Stats), C.c_void_p]
+        lib.fdgpu_probe_fp64.argtypes = [P, C.POINTER(C.c_double)]
         lib.fdgpu_velocity_to_slowness.argtypes = [P, C.c_void_p, C.c_void_p, C.c_longlong, C.c_void_p]
         lib.fdgpu_sphfd.argtypes = [C.c_int, C.POINTER(C.c_char_p), C.c_char_p]
         lib.fdgpu_sphfd_parlist.argtypes = [C.c_int, C.POINTER(C.c_char_p), C.c_char_p, C.POINTER(C.c_int)]
@@ -157,6 +160,12 @@ class Context:
                                          1 if initialised else 0, stats, C.c_void_p(stream_ptr))
         _check(rc, self.ptr)
         return [s.as_dict() for s in stats]
+
+    def probe_fp64_gops(self) -> float:
+        """Measured FP64 instruction rate (G instructions/s) of this GPU."""
+        g = C.c_double()
+        _check(self.lib.fdgpu_probe_fp64(self.ptr, C.byref(g)), self.ptr)
+        return g.value
 
     def velocity_to_slowness(self, vel_ptr: int, slow_ptr: int, n: int, stream_ptr: int = 0):
         _check(self.lib.fdgpu_velocity_to_slowness(self.ptr, C.c_void_p(vel_ptr), C.c_void_p(slow_ptr), n,

@@ -72,6 +72,9 @@ typedef struct {
     int64_t deferred;        /* points that took the stale (t0,t4) of an earlier point */
     int64_t stencils[5];     /* stencil evaluations: 3-D, new-edge, 2-D, new-face, 1-D */
     int32_t restart_wall[8]; /* restarts per wall 1..6 */
+    int64_t phase_cycles[6]; /* profiling builds only: cycles in face set-up, the three evaluation
+                                phases, round bookkeeping and deferred resolution */
+    int64_t t_start_ns, t_end_ns; /* GPU global timer (ns) at the start and end of this solve */
 } fdgpu_stats;
 
 int fdgpu_create(int device, fdgpu_ctx **out);
@@ -104,6 +107,11 @@ int fdgpu_solve_device(fdgpu_ctx *ctx, int n, const fdgpu_station *st, const flo
 /* velocity -> slowness on the device, slow[i] = 1/v[i] as the reference rounds it (src/sphfd.c:689) */
 int fdgpu_velocity_to_slowness(fdgpu_ctx *ctx, const float *d_velocity, float *d_slowness, long long n,
                                void *stream);
+
+/* Diagnostics: measured FP64 instruction rate of this GPU (fused multiply-adds per second / 1e9),
+ * the denominator the benchmark reports the solver's FP64 throughput against.  No counterpart in
+ * the reference. */
+int fdgpu_probe_fp64(fdgpu_ctx *ctx, double *gops);
 
 /* Drop-in sphfd(): ac/av as the reference's (av[1] = "par=<file>"), output_path = timedir.
  * Reads the velocity file, solves on the GPU, writes <output_path>/<timefile> byte-for-byte as
