@@ -1,0 +1,80 @@
+"""The CPU oracle against the reference's own outputs (golden fixtures made by
+tests/golden/make_golden.py from the reference binary)."""
+import hashlib
+import json
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from cases import random_case, write_random_case
+from oracle_util import ORACLE_DIR, run_oracle
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+REF_BIN = os.path.join(ORACLE_DIR, "_ref", "sphfd_ref")
+
+
+def _sha(path):
+    return hashlib.sha256(open(path, "rb").read()).hexdigest()
+
+
+def _m001_case(tmp_path):
+    from fdtomoc_gb300.formats import write_par
+    z = np.load(os.path.join(GOLDEN, "m001.npz"))
+    vf = tmp_path / "m001.vel"
+    vf.write_bytes(z["velocity_file"].tobytes())
+    meta = json.load(open(os.path.join(GOLDEN, "reference_outputs.json")))["m001"]
+    pf = str(tmp_path / "M001.par")
+    write_par(pf, dict(meta["par"], velfile=str(vf)))
+    return pf, z["expected"].tobytes()
+
+
+@pytest.mark.parametrize("fast", [False, True])
+def test_m001_reference_golden(oracle_lib, tmp_path, fast):
+    """The reference's verification/cmod/M001.ptimes, reproduced byte for byte."""
+    pf, expected = _m001_case(tmp_path)
+    run_oracle(pf, str(tmp_path / "out"), fast=fast)
+    assert (tmp_path / "out" / "M001.ptimes").read_bytes() == expected
+
+
+REF = json.load(open(os.path.join(GOLDEN, "reference_outputs.json")))
+
+
+@pytest.mark.parametrize("seed", sorted(int(s) for s in REF["cases"]))
+def test_seeded_cases_match_reference(oracle_lib, tmp_path, seed):
+    pf = write_random_case(random_case(seed), str(tmp_path))
+    st = run_oracle(pf, str(tmp_path / "out"), fast=True)
+    assert _sha(tmp_path / "out" / "case.ptimes") == REF["cases"][str(seed)]["sha256"]
+    assert st.sweeps == REF["cases"][str(seed)]["sweeps"]
+
+
+def test_literal_and_fast_modes_agree(oracle_lib, tmp_path):
+    """The pruned / tabled evaluation (the GPU's arithmetic plan) equals the literal restatement."""
+    for seed in (2, 9, 33):
+        pf = write_random_case(random_case(seed), str(tmp_path / str(seed)))
+        run_oracle(pf, str(tmp_path / str(seed) / "lit"), fast=False)
+        run_oracle(pf, str(tmp_path / str(seed) / "fast"), fast=True)
+        assert _sha(tmp_path / str(seed) / "lit" / "case.ptimes") == _sha(tmp_path / str(seed) / "fast" / "case.ptimes")
+
+
+def test_config1_matches_reference(oracle_lib, tmp_path):
+    from fdtomoc_gb300 import workloads as W
+    g, v, sts = W.config(1)
+    W.write_case(str(tmp_path), g, v, sts)
+    run_oracle(str(tmp_path / "S0000.par"), str(tmp_path / "orc"), fast=True)
+    assert _sha(tmp_path / "orc" / "S0000.ptimes") == REF["config1_S0000"]["sha256"]
+
+
+@pytest.mark.skipif(not os.path.exists(REF_BIN), reason="reference sources not present here")
+@pytest.mark.parametrize("seed", [500, 501, 502, 503, 504, 505])
+def test_live_reference_vs_oracle(oracle_lib, tmp_path, seed):
+    """Fresh seeds, the reference binary itself against the oracle."""
+    pf = write_random_case(random_case(seed), str(tmp_path))
+    out = tmp_path / "ref"
+    out.mkdir()
+    (tmp_path / "pl").write_text("par=" + pf + "\n")
+    (tmp_path / "spec").write_text(f"parlist {tmp_path / 'pl'}\ntimedir {out}\n")
+    subprocess.run([REF_BIN], input=str(tmp_path / "spec") + "\n", capture_output=True, text=True, check=True)
+    run_oracle(pf, str(tmp_path / "orc"), fast=True)
+    assert _sha(out / "case.ptimes") == _sha(tmp_path / "orc" / "case.ptimes")
