@@ -250,6 +250,7 @@ extern "C" const char *fdgpu_strerror(int s)
     case FDGPU_ESOURCE: return "source outside the grid";
     case FDGPU_ESCHED: return "face walk exceeded its bound";
     case FDGPU_ENODEV: return "no CUDA device";
+    case FDGPU_ETOOBIG: return "problem exceeds the static scratch of the no-allocation entry point";
     default: return "unknown status";
     }
 }

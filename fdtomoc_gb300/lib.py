@@ -15,7 +15,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.environ.get("FDGPU_LIB") or os.path.join(HERE, "libfdgpu.so")
 
 FDGPU_OK = 0
-ERRORS = {-1: "EINVAL", -2: "ENOMEM", -3: "ECUDA", -4: "EIO", -5: "EPAR", -6: "ESOURCE", -7: "ESCHED", -8: "ENODEV"}
+ERRORS = {-1: "EINVAL", -2: "ENOMEM", -3: "ECUDA", -4: "EIO", -5: "EPAR", -6: "ESOURCE", -7: "ESCHED", -8: "ENODEV",
+          -9: "ETOOBIG"}
 
 
 class Station(C.Structure):

@@ -37,7 +37,8 @@ enum {
     FDGPU_EPAR = -5,     /* a required par parameter is missing or a value is invalid */
     FDGPU_ESOURCE = -6,  /* the source is outside the grid (src/sphfd.c:533-538) */
     FDGPU_ESCHED = -7,   /* internal: a face walk exceeded its round bound */
-    FDGPU_ENODEV = -8    /* no CUDA device */
+    FDGPU_ENODEV = -8,   /* no CUDA device */
+    FDGPU_ETOOBIG = -9   /* the problem needs more than fdgpu_solve_noalloc's static scratch */
 };
 
 typedef struct fdgpu_ctx fdgpu_ctx;
@@ -112,6 +113,23 @@ int fdgpu_velocity_to_slowness(fdgpu_ctx *ctx, const float *d_velocity, float *d
  * the denominator the benchmark reports the solver's FP64 throughput against.  No counterpart in
  * the reference. */
 int fdgpu_probe_fp64(fdgpu_ctx *ctx, double *gops);
+
+/* Solve one point-source station without allocating device memory.  It has no counterpart in the
+ * reference: it is for callers that must not have a library call cudaMalloc / cudaFree.  Such
+ * callers include loops that cannot afford the device-wide synchronisation cudaFree implies, and
+ * applications whose device memory belongs to another allocator.  The caller passes the slowness
+ * model (strides 1, s_sy, s_sz; the station reads its window at ox, oy, oz) and the output field
+ * (nx*ny*nz floats), both device buffers it owns.  All other scratch (station descriptor,
+ * statistics, geometry tables, face-walk scratch) lives in one static device array of
+ * FDGPU_NOALLOC_SCRATCH_BYTES per GPU, held from library load to process exit.  A station that needs
+ * more returns FDGPU_ETOOBIG before any GPU work; a 201x201x81 grid needs about 12 MiB.  The first
+ * call on a device looks up the array's address; make it before any stream capture.  Calls share the
+ * array, so calls that overlap on one GPU race: serialise them per device.  The call returns when the
+ * solve has finished on `stream` (a cudaStream_t, NULL = default stream); results are bit-identical
+ * to fdgpu_solve_device. */
+#define FDGPU_NOALLOC_SCRATCH_BYTES (16u << 20)
+int fdgpu_solve_noalloc(const fdgpu_station *st, const float *d_slowness, long long s_sy, long long s_sz,
+                        float *d_time, fdgpu_stats *stats, void *stream);
 
 /* Drop-in sphfd(): ac/av as the reference's (av[1] = "par=<file>"), output_path = timedir.
  * Reads the velocity file, solves on the GPU, writes <output_path>/<timefile> byte-for-byte as
