@@ -297,8 +297,11 @@ extern "C" int fdgpu_solve_device(fdgpu_ctx *ctx, int n, const fdgpu_station *st
     }
     /* scratch and per-station records */
     std::vector<size_t> off(n + 1, 0);
+    /* per station: face scratch, then the plane-pipelining arrays (9 bytes per grid node) */
+    auto nodes = [&](int k) { return (size_t)st[k].nx * st[k].ny * st[k].nz; };
     for (int k = 0; k < n; k++)
-        off[k + 1] = off[k] + ((((size_t)max_face(st[k]) + 16) * kScratchPerPoint + 255) & ~(size_t)255);
+        off[k + 1] = off[k] + ((((size_t)max_face(st[k]) + 16) * kScratchPerPoint + 255) & ~(size_t)255)
+                     + ((nodes(k) * 9 + 255 + 512) & ~(size_t)255);
     FD_CU(ctx, ctx->scratch.ensure(off[n]));
     FD_CU(ctx, ctx->stations.ensure(sizeof(fd_station_dev) * n));
     FD_CU(ctx, ctx->stats.ensure(sizeof(fd_station_stats) * n));
@@ -357,6 +360,13 @@ extern "C" int fdgpu_solve_device(fdgpu_ctx *ctx, int n, const fdgpu_station *st
         d.scr.wl[1] = reinterpret_cast<int *>(base + 24 * m);
         d.scr.deferred = reinterpret_cast<int *>(base + 28 * m);
         d.scr.dag = reinterpret_cast<unsigned char *>(base + 32 * m);
+        {
+            char *pb = base + ((((size_t)m + 16) * kScratchPerPoint + 255) & ~(size_t)255);
+            const size_t nn = nodes(k);
+            d.scr.pcount = reinterpret_cast<unsigned *>(pb);
+            d.scr.pqueue = reinterpret_cast<int *>(pb + 4 * nn);
+            d.scr.pemask = reinterpret_cast<unsigned char *>(pb + 8 * nn);
+        }
         d.max_face_pad = ((long long)m + 15) & ~15LL;
         max_pad = std::max(max_pad, d.max_face_pad);
         d.stats = ctx->stats.as<fd_station_stats>() + k;

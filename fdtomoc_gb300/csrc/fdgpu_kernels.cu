@@ -137,6 +137,9 @@ struct Shared {
     int sweeps;
     int restart_wall[8];
     long long cyc[6];
+    /* plane-pipelined sweep: number of planes, layer of plane 0, queue tail, done flag */
+    int pipelined, np, player0, qtail;
+    long long psweeps;
 };
 
 /* face frame for a face number known only at run time */
@@ -228,6 +231,8 @@ struct Smem {
     float t[FD_CHUNK][NB_N];
     float s[FD_CHUNK][NB_N];
     int idx[FD_CHUNK];               /* fill index of the chunk's point */
+    int lay[FD_CHUNK];               /* its face layer */
+    int pl[FD_CHUNK];                /* its plane in a pipelined sweep (-1 otherwise) */
     int z[FD_CHUNK], y[FD_CHUNK];
     unsigned guardm[FD_CHUNK];       /* trials whose guards pass (first-contact gates excluded) */
     unsigned evalm[FD_CHUNK];        /* trials whose value was computed in the parallel phases */
@@ -457,6 +462,96 @@ __device__ void run_items(const fd_station_dev &sd, Smem &sm, int k0, int k1, Co
     }
 }
 
+/* ---------------------------------------------------------------------------------------------- */
+/* plane-pipelined sweeps                                                                          */
+/*                                                                                                 */
+/* After a restart the box is one whole model wall and a sweep is a run of full planes, each one's */
+/* inner layer being the previous plane (src/sphfd.c:5623-5674).  A point of plane p+1 needs only  */
+/* the 3x3 block below it in plane p and its earlier neighbours in its own plane; so the planes    */
+/* are walked as one dependency graph instead of one after the other.  Every node has one counter  */
+/* word: inner-layer nodes pending in bits 0-7, in-plane neighbours pending in bits 8-15.  When a   */
+/* node's inner block is complete, the keys of its in-plane neighbours (their inner-layer times)   */
+/* are final, so it learns which neighbours come later and drops them from its count; earlier      */
+/* neighbours drop themselves when they finish.  The word reaching zero queues the node.  The run */
+/* is taken only when no point can need an earlier point's stencil state (see fd_solve).          */
+
+__device__ __forceinline__ unsigned long long node_key(float tin, int i)
+{
+    return ((unsigned long long)okey32(tin) << 32) | (unsigned)i;
+}
+
+/* earlier-neighbour byte of fill index i, keys from the inner-layer field at `inner_layer` */
+__device__ unsigned earlier_mask(const fd_station_dev &sd, const Shared &sh, int i, int inner_layer)
+{
+    const fdn_frame fr = frame_of(sh.face);
+    const int nvf = sh.n / sh.nuf, iu = i % sh.nuf, iv = i / sh.nuf;
+    auto tin = [&](int ju, int jv) {
+        int xyz[3];
+        xyz[fr.axis_u] = sh.ulo + ju;
+        xyz[fr.axis_v] = sh.vlo + jv;
+        xyz[fr.axis_n] = inner_layer;
+        return sd.T[((long long)xyz[2] * sd.g.ny + xyz[1]) * sd.g.nx + xyz[0]];
+    };
+    const unsigned long long ki = node_key(tin(iu, iv), i);
+    unsigned em = 0;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        int du, dv;
+        nb_off(k, du, dv);
+        const int ju = iu + du, jv = iv + dv;
+        if (ju < 0 || ju >= sh.nuf || jv < 0 || jv >= nvf) continue;
+        if (node_key(tin(ju, jv), jv * sh.nuf + ju) < ki) em |= 1u << k;
+    }
+    return em;
+}
+
+/* node (plane pp, fill index i) is final: record (last plane), release its later in-plane
+ * neighbours and the plane pp+1 nodes whose inner block contains it */
+__device__ void pipelined_release(const fd_station_dev &sd, Shared &sh, int slot, int i, int pp, bool writer,
+                                  float st0, float st4, const float *t18)
+{
+    const int nplane = sh.n, nvf = sh.n / sh.nuf, iu = i % sh.nuf, iv = i / sh.nuf;
+    const fdn_frame fr = frame_of(sh.face);
+    if (pp == sh.np - 1) {
+        if (writer) {
+            sd.scr.rec[i] = make_float2(st0, st4);
+            atomicMax(&sh.exitkey, node_key(t18[13], i));
+        } else {
+            sd.scr.rec[i] = make_float2(__int_as_float(0x7fc00000), __int_as_float(0x7fc00000));
+        }
+    }
+    const long long base = (long long)pp * nplane;
+    unsigned later = inrect_mask(iu, iv, sh.nuf, nvf) & ~(unsigned)sd.scr.pemask[base + i];
+    while (later) {
+        const int k = __ffs(later) - 1;
+        later &= later - 1;
+        int du, dv;
+        nb_off(k, du, dv);
+        const int j = (iv + dv) * sh.nuf + iu + du;
+        const unsigned old = atomicSub(&sd.scr.pcount[base + j], 1u << 8);
+        if (old == (1u << 8)) sd.scr.pqueue[atomicAdd(&sh.qtail, 1)] = (int)(base + j);
+    }
+    if (pp + 1 < sh.np) {
+        const long long nb = base + nplane;
+        const int layer = sh.player0 - pp * fr.inner;   /* this plane = the next plane's inner layer */
+        for (int dv = -1; dv <= 1; dv++)
+            for (int du = -1; du <= 1; du++) {
+                const int ju = iu + du, jv = iv + dv;
+                if (ju < 0 || ju >= sh.nuf || jv < 0 || jv >= nvf) continue;
+                const int j = jv * sh.nuf + ju;
+                const unsigned old = atomicSub(&sd.scr.pcount[nb + j], 1u);
+                if ((old & 0xFFu) != 1u) continue;
+                /* inner block of node j complete: its in-plane order is now known */
+                const unsigned em = earlier_mask(sd, sh, j, layer);
+                sd.scr.pemask[nb + j] = (unsigned char)em;
+                const unsigned lat = (unsigned)__popc(inrect_mask(ju, jv, sh.nuf, nvf) & ~em);
+                const unsigned w = old - 1u;
+                const unsigned prev = lat ? atomicSub(&sd.scr.pcount[nb + j], lat << 8) : w;
+                if (prev - (lat << 8) == 0u) sd.scr.pqueue[atomicAdd(&sh.qtail, 1)] = (int)(nb + j);
+            }
+    }
+}
+
 /* Phase C for one point: the reference's sequential minimum over the 22 trials, from the values
  * computed in the parallel phases (new-edge and new-face values that were not precomputed are
  * evaluated here — they are needed only at first contact), then the commit
@@ -470,7 +565,10 @@ __device__ bool phase_c(const fd_station_dev &sd, Shared &sh, Smem &sm, int slot
     const unsigned gm = sm.guardm[slot], em = sm.evalm[slot];
     const double told = f2d(t18[NB_POINT]);
     /* a 2-D trial before any corner / new-edge call would read the previous point's t0,t4 */
-    if (!have_inherit && (gm & 0xFu) == 0 && !((gm & 0xF0u) && told > 1.0e9) && (gm & 0xFF00u)) return false;
+    if (!have_inherit && (gm & 0xFu) == 0 && !((gm & 0xF0u) && told > 1.0e9) && (gm & 0xFF00u)) {
+        if (sh.pipelined) sh.status = 6;   /* excluded by the pipelining precondition */
+        return false;
+    }
     const int z = sm.z[slot], y = sm.y[slot];
     double guess = told;
     float st0 = it0, st4 = it4;
@@ -530,7 +628,7 @@ __device__ bool phase_c(const fd_station_dev &sd, Shared &sh, Smem &sm, int slot
         int xyz[3];
         xyz[fr.axis_u] = sh.ulo + i % sh.nuf;
         xyz[fr.axis_v] = sh.vlo + i / sh.nuf;
-        xyz[fr.axis_n] = sh.layer;
+        xyz[fr.axis_n] = sm.lay[slot];
         const long long pT = ((long long)xyz[2] * sd.g.ny + xyz[1]) * sd.g.nx + xyz[0];
         sd.T[pT] = __double2float_rn(guess);
         if (lastK >= 0) {
@@ -538,6 +636,10 @@ __device__ bool phase_c(const fd_station_dev &sd, Shared &sh, Smem &sm, int slot
             const double fhead = (last_gb - last_v) / head_den(sm.desc[lastK], s18, sd.g, z, y);
             if (fhead > FD_HEADTEST) atomicAdd(&sh.headw[fr.headw], 1);
         }
+    }
+    if (sh.pipelined) {
+        pipelined_release(sd, sh, slot, i, sm.pl[slot], writers != 0, st0, st4, t18);
+        return true;
     }
     if (writers) {
         sd.scr.rec[i] = make_float2(st0, st4);
@@ -586,16 +688,22 @@ __device__ void run_chunk(const fd_station_dev &sd, Shared &sh, Smem &sm, const 
     const fdn_frame fr = frame_of(sh.face);
     for (int r = tid; r < m * FD_TPP; r += blockDim.x) {
         const int slot = r / FD_TPP, q = r % FD_TPP;
-        const int i = list[slot];
+        /* list entries: fill indices, or plane*n + fill index in a pipelined sweep */
+        const int e = list[slot];
+        const int pp = sh.pipelined ? e / sh.n : -1;
+        const int i = sh.pipelined ? e - pp * sh.n : e;
+        const int layer = sh.pipelined ? sh.player0 - pp * fr.inner : sh.layer;
         const int u = sh.ulo + i % sh.nuf, v = sh.vlo + i / sh.nuf;
         int xyz[3];
         xyz[fr.axis_u] = u;
         xyz[fr.axis_v] = v;
-        xyz[fr.axis_n] = sh.layer;
+        xyz[fr.axis_n] = layer;
         const long long pT = ((long long)xyz[2] * sd.g.ny + xyz[1]) * sd.g.nx + xyz[0];
         const long long pS = (long long)xyz[2] * sd.s_sz + (long long)xyz[1] * sd.s_sy + xyz[0];
         if (q == 0) {
             sm.idx[slot] = i;
+            sm.lay[slot] = layer;
+            sm.pl[slot] = pp;
             sm.z[slot] = xyz[2];
             sm.y[slot] = xyz[1];
             sm.guardm[slot] = 0;
@@ -748,6 +856,121 @@ __device__ void face_walk(const fd_station_dev &sd, Shared &sh, Smem &sm, bool d
     }
 }
 
+/* face parameters of face `face` for the current walls (thread 0) */
+__device__ void setup_face(const fd_station_dev &sd, Shared &sh, int face)
+{
+    const int nx = sd.g.nx, ny = sd.g.ny, nz = sd.g.nz;
+    const long long nxy = (long long)nx * ny;
+    /* walls: 0 z1, 1 z2, 2 x2, 3 x1, 4 y1, 5 y2 */
+    const int x1 = sh.wall[3], x2 = sh.wall[2], y1 = sh.wall[4], y2 = sh.wall[5];
+    const int z1 = sh.wall[0], z2 = sh.wall[1];
+    sh.face = face;
+    sh.layer = sh.wall[face];
+    if (face < 2) {
+        sh.ulo = x1 + 1; sh.uhi = x2 - 1; sh.vlo = y1 + 1; sh.vhi = y2 - 1;
+        sh.nu = nx; sh.nv = ny;
+        sh.su = 1; sh.sv = nx; sh.sn = nxy;
+        sh.ssu = 1; sh.ssv = sd.s_sy; sh.ssn = sd.s_sz;
+    } else if (face < 4) {
+        sh.ulo = y1 + 1; sh.uhi = y2 - 1; sh.vlo = z1 + 1; sh.vhi = z2 - 1;
+        sh.nu = ny; sh.nv = nz;
+        sh.su = nx; sh.sv = nxy; sh.sn = 1;
+        sh.ssu = sd.s_sy; sh.ssv = sd.s_sz; sh.ssn = 1;
+    } else {
+        sh.ulo = x1 + 1; sh.uhi = x2 - 1; sh.vlo = z1 + 1; sh.vhi = z2 - 1;
+        sh.nu = nx; sh.nv = nz;
+        sh.su = 1; sh.sv = nxy; sh.sn = nx;
+        sh.ssu = 1; sh.ssv = sd.s_sz; sh.ssn = sd.s_sy;
+    }
+    sh.nuf = sh.uhi - sh.ulo + 1;
+    const int nvf = sh.vhi - sh.vlo + 1;
+    sh.n = (sh.nuf > 0 && nvf > 0) ? sh.nuf * nvf : 0;
+    sh.n_pad = (sh.n + 15) & ~15;
+}
+
+/* One sweep of face F as a plane-pipelined dependency graph.  Leaves walls, flags and radius as
+ * the radius loop of src/sphfd.c:1018-5566 would. */
+__device__ void pipelined_sweep(const fd_station_dev &sd, Shared &sh, Smem &sm, Counters &cn, int F)
+{
+    const int tid = threadIdx.x;
+    const fdn_frame fr = frame_of(F);
+    if (tid == 0) {
+        setup_face(sd, sh, F);
+        /* the planes the radius loop would visit: up to grow[F] per radius step, until the wall
+         * reaches the model side or the radius reaches maxrad */
+        const int nmax = F < 2 ? sd.g.nz : F < 4 ? sd.g.nx : sd.g.ny;
+        int w = sh.wall[F], flag = sh.dflag[F], radius = sh.radius, rad0 = sh.rad0, np = 0;
+        while (rad0 && flag) {
+            for (int ig = 1; ig <= sd.grow[F]; ig++) {
+                if (!flag) continue;
+                np++;
+                if (fr.inner > 0 ? (w == 0) : (w == nmax - 1)) flag = 0;
+                w -= fr.inner;
+            }
+            radius++;
+            if (radius == sd.maxrad) rad0 = 0;
+        }
+        sh.np = np;
+        sh.player0 = sh.wall[F];
+        sh.wall[F] = w;
+        sh.dflag[F] = flag;
+        sh.radius = radius;
+        sh.rad0 = rad0;
+        sh.qtail = 0;
+        sh.exitkey = 0ull;
+        sh.pipelined = 1;
+    }
+    for (int k = tid; k < FDN_NTRIAL; k += blockDim.x) sm.desc[k] = c_desc[F * FDN_NTRIAL + k];
+    __syncthreads();
+    const int np = sh.np, nplane = sh.n, nuf = sh.nuf, nvf = nplane > 0 ? nplane / nuf : 0;
+    const long long total = (long long)np * nplane;
+    if (total > 0) {
+        /* counters: plane 0 reads the static wall layer, so its in-plane order is known now */
+        const int wall_layer = sh.player0 + fr.inner;
+        for (long long id = tid; id < total; id += blockDim.x) {
+            const int pp = (int)(id / nplane), i = (int)(id - (long long)pp * nplane);
+            const unsigned inr = inrect_mask(i % nuf, i / nuf, nuf, nvf);
+            const unsigned c2 = (unsigned)__popc(inr);
+            unsigned wd = (pp > 0 ? 1u + c2 : 0u) | (c2 << 8);
+            if (pp == 0) {
+                const unsigned em = earlier_mask(sd, sh, i, wall_layer);
+                sd.scr.pemask[id] = (unsigned char)em;
+                wd -= (unsigned)__popc(inr & ~em) << 8;
+            }
+            sd.scr.pcount[id] = wd;
+            if (wd == 0u) sd.scr.pqueue[atomicAdd(&sh.qtail, 1)] = (int)id;
+        }
+        long long head = 0, steps = 0;
+        for (;;) {
+            __syncthreads();
+            const long long tail = sh.qtail;
+            if (head >= total || sh.status) break;
+            const long long avail = tail - head;
+            if (avail <= 0 || ++steps > total + 8) {
+                if (tid == 0) sh.status = 5;   /* cannot happen: every node is queued exactly once */
+                break;
+            }
+            const int m = avail < FD_CHUNK ? (int)avail : FD_CHUNK;
+            run_chunk(sd, sh, sm, sd.scr.pqueue + head, m, false, 0.f, 0.f, 0, sd.scr.dag, cn);
+            head += m;
+        }
+        __syncthreads();
+        if (tid == 0) sh.rounds += steps;
+    }
+    if (tid == 0) {
+        if (sh.exitkey) {
+            const float2 r = sd.scr.rec[(int)(sh.exitkey & 0xffffffffu)];
+            sh.carry_t0 = r.x;
+            sh.carry_t4 = r.y;
+        }
+        sh.faces += np;
+        sh.node_updates += total;
+        sh.psweeps++;
+        sh.pipelined = 0;
+    }
+    __syncthreads();
+}
+
 /* ---------------------------------------------------------------------------------------------- */
 /* source box (src/sphfd.c:724-825)                                                                */
 
@@ -814,6 +1037,8 @@ __global__ void __launch_bounds__(FD_BLOCK, 1) fd_solve(const fd_station_dev *st
         sh.sweeps = 0;
         for (int k = 0; k < 8; k++) sh.restart_wall[k] = 0;
         for (int k = 0; k < 6; k++) sh.cyc[k] = 0;
+        sh.pipelined = 0;
+        sh.psweeps = 0;
     }
     __syncthreads();
     Counters cn;
@@ -824,38 +1049,33 @@ __global__ void __launch_bounds__(FD_BLOCK, 1) fd_solve(const fd_station_dev *st
     while (sh.reverse > -1 && sh.status == 0) {
         if (tid == 0) for (int k = 0; k < 8; k++) sh.headw[k] = 0;
         __syncthreads();
-        while (sh.rad0 && (sh.dflag[0] || sh.dflag[1] || sh.dflag[2] || sh.dflag[3] || sh.dflag[4] || sh.dflag[5])
+        /* A sweep with one active face (every sweep after a restart) walks full planes.  It runs as
+         * one plane-pipelined graph when no point can need an earlier point's stencil state: every
+         * time below 1e9 makes every corner guard that is inside the grid pass (so each point calls
+         * a corner stencil before its 2-D trials), except the EAST corner whose guard tests the node
+         * above for being non-zero (src/sphfd.c:2544), which fails only next to a zero time. */
+        int act = -1, nact = 0;
+        for (int f = 0; f < 6; f++)
+            if (sh.dflag[f]) { act = f; nact++; }
+        bool piped = false;
+        if (nact == 1 && sh.rad0 && sd.scr.pcount) {
+            int bad = 0;
+            const long long nxyz = nxy * nz;
+            for (long long i = tid; i < nxyz; i += blockDim.x) {
+                const float t = sd.T[i];
+                if (!(t < 1.e9f)) bad = 1;
+                else if (act == 2 && t == 0.0f && (i / nx) % ny == 0 && i / nxy == 1) bad = 1;
+            }
+            piped = !__syncthreads_or(bad);
+        }
+        if (piped) pipelined_sweep(sd, sh, sm, cn, act);
+        while (!piped && sh.rad0
+               && (sh.dflag[0] || sh.dflag[1] || sh.dflag[2] || sh.dflag[3] || sh.dflag[4] || sh.dflag[5])
                && sh.status == 0) {
             for (int face = 0; face < 6; face++) {
                 for (int ig = 1; ig <= sd.grow[face]; ig++) {
                     if (!sh.dflag[face]) continue;
-                    if (tid == 0) {
-                        /* walls: 0 z1, 1 z2, 2 x2, 3 x1, 4 y1, 5 y2 */
-                        const int x1 = sh.wall[3], x2 = sh.wall[2], y1 = sh.wall[4], y2 = sh.wall[5];
-                        const int z1 = sh.wall[0], z2 = sh.wall[1];
-                        sh.face = face;
-                        sh.layer = sh.wall[face];
-                        if (face < 2) {
-                            sh.ulo = x1 + 1; sh.uhi = x2 - 1; sh.vlo = y1 + 1; sh.vhi = y2 - 1;
-                            sh.nu = nx; sh.nv = ny;
-                            sh.su = 1; sh.sv = nx; sh.sn = nxy;
-                            sh.ssu = 1; sh.ssv = sd.s_sy; sh.ssn = sd.s_sz;
-                        } else if (face < 4) {
-                            sh.ulo = y1 + 1; sh.uhi = y2 - 1; sh.vlo = z1 + 1; sh.vhi = z2 - 1;
-                            sh.nu = ny; sh.nv = nz;
-                            sh.su = nx; sh.sv = nxy; sh.sn = 1;
-                            sh.ssu = sd.s_sy; sh.ssv = sd.s_sz; sh.ssn = 1;
-                        } else {
-                            sh.ulo = x1 + 1; sh.uhi = x2 - 1; sh.vlo = z1 + 1; sh.vhi = z2 - 1;
-                            sh.nu = nx; sh.nv = nz;
-                            sh.su = 1; sh.sv = nxy; sh.sn = nx;
-                            sh.ssu = 1; sh.ssv = sd.s_sz; sh.ssn = sd.s_sy;
-                        }
-                        sh.nuf = sh.uhi - sh.ulo + 1;
-                        const int nvf = sh.vhi - sh.vlo + 1;
-                        sh.n = (sh.nuf > 0 && nvf > 0) ? sh.nuf * nvf : 0;
-                        sh.n_pad = (sh.n + 15) & ~15;
-                    }
+                    if (tid == 0) setup_face(sd, sh, face);
                     __syncthreads();
                     if (sh.n > 0) face_walk(sd, sh, sm, dag_in_smem, cn);
                     __syncthreads();

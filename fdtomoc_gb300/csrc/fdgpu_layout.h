@@ -82,6 +82,12 @@ typedef struct {
     int *deferred;             /* points waiting for an earlier point's (t0,t4) */
     unsigned char *dag;        /* in-degree and earlier-neighbour bytes (2 per point) when they do
                                   not fit in shared memory */
+    /* plane-pipelined sweeps (NULL: not available, every face is walked on its own):
+     * one word per grid node (inner-layer dependencies pending in bits 0-7, in-plane ones in 8-15),
+     * the sweep's ready queue and each node's earlier-neighbour byte */
+    unsigned *pcount;
+    int *pqueue;
+    unsigned char *pemask;
 } fd_scratch_dev;
 
 typedef struct {

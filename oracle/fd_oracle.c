@@ -480,7 +480,32 @@ static void fdo_run_face(fdo_face *F, fdo_sortent *buf, fdo_carry *carry, int *h
         const int u = F->ulo + buf[i].idx % nu, v = F->vlo + buf[i].idx / nu;
         fdo_point(F, u, v, carry, headw);
     }
-    if (F->st) { F->st->node_updates += n; F->st->faces++; }
+    if (F->st) {
+        F->st->node_updates += n;
+        F->st->faces++;
+        if (F->st->sweeps < 64) {
+            /* dependency depth: level = 1 + max level of earlier in-face neighbours, in sort order */
+            int *lev = (int *)calloc((size_t)n, sizeof(int)), *pos = (int *)malloc(sizeof(int) * (size_t)n);
+            for (int i = 0; i < n; i++) pos[buf[i].idx] = i;
+            int depth = 0;
+            for (int i = 0; i < n; i++) {
+                const int id = buf[i].idx, iu = id % nu, iv = id / nu;
+                int l = 1;
+                for (int dv = -1; dv <= 1; dv++)
+                    for (int du = -1; du <= 1; du++) {
+                        const int ju = iu + du, jv = iv + dv;
+                        if ((du || dv) && ju >= 0 && ju < nu && jv >= 0 && jv < nvv && pos[jv * nu + ju] < i)
+                            if (lev[jv * nu + ju] + 1 > l) l = lev[jv * nu + ju] + 1;
+                    }
+                lev[id] = l;
+                if (l > depth) depth = l;
+            }
+            F->st->depth_per_sweep[F->st->sweeps] += depth;
+            F->st->updates_per_sweep[F->st->sweeps] += n;
+            free(lev);
+            free(pos);
+        }
+    }
 }
 
 int fdo_headpref(const fdo_grid *g, const fdo_box *b, int headpref)

@@ -50,6 +50,9 @@ typedef struct {
     int sweeps;
     int restarts[7];          /* restart wall chosen after each sweep, by wall number (count) */
     int64_t changed_per_sweep[64];
+    int64_t depth_per_sweep[64];  /* sum over the sweep's faces of the face's dependency depth (longest
+                                     chain of in-face neighbours in sort order) */
+    int64_t updates_per_sweep[64];
 } fdo_stats;
 
 /* Stale stencil state: the (t[0], t[4]) pair that fdsph2d reads but no 2-D call site assigns. */

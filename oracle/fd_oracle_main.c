@@ -47,7 +47,10 @@ int main(void)
         memset(&st, 0, sizeof st);
         int rc = fdo_sphfd(2, av, timedir, mode, &st);
         if (rc) { fprintf(stderr, "%s: error %d\n", line, rc); failures++; continue; }
-        if (getenv("FDO_CHANGED")) { for (int k = 0; k < st.sweeps && k < 64; k++) fprintf(stderr, "sweep %d changed %lld\n", k, (long long)st.changed_per_sweep[k]); }
+        if (getenv("FDO_CHANGED"))
+            for (int k = 0; k < st.sweeps && k < 64; k++)
+                fprintf(stderr, "sweep %d changed %lld updates %lld depth %lld\n", k, (long long)st.changed_per_sweep[k],
+                        (long long)st.updates_per_sweep[k], (long long)st.depth_per_sweep[k]);
         fprintf(stderr, "%s: sweeps=%d node_updates=%lld faces=%lld inherit=%lld calls=%lld/%lld/%lld/%lld/%lld skipped=%lld/%lld/%lld/%lld\n",
                 line, st.sweeps, (long long)st.node_updates, (long long)st.faces, (long long)st.inherit_points,
                 (long long)st.calls[0], (long long)st.calls[1], (long long)st.calls[2], (long long)st.calls[3],

@@ -11,7 +11,8 @@ _lib = None
 class OracleStats(C.Structure):
     _fields_ = [("node_updates", C.c_int64), ("calls", C.c_int64 * 5), ("skipped", C.c_int64 * 5),
                 ("inherit_points", C.c_int64), ("faces", C.c_int64), ("sweeps", C.c_int),
-                ("restarts", C.c_int * 7), ("changed_per_sweep", C.c_int64 * 64)]
+                ("restarts", C.c_int * 7), ("changed_per_sweep", C.c_int64 * 64),
+                ("depth_per_sweep", C.c_int64 * 64), ("updates_per_sweep", C.c_int64 * 64)]
 
 
 def load_oracle():
