@@ -355,10 +355,9 @@ extern "C" int fdgpu_solve_device(fdgpu_ctx *ctx, int n, const fdgpu_station *st
         const size_t m = (size_t)max_face(s);
         d.scr.key = reinterpret_cast<unsigned long long *>(base);
         d.scr.rec = reinterpret_cast<float2 *>(base + 8 * m);
-        d.scr.indeg = reinterpret_cast<int *>(base + 16 * m);
-        d.scr.wl[0] = reinterpret_cast<int *>(base + 20 * m);
-        d.scr.wl[1] = reinterpret_cast<int *>(base + 24 * m);
-        d.scr.deferred = reinterpret_cast<int *>(base + 28 * m);
+        d.scr.pst = reinterpret_cast<int *>(base + 16 * m);
+        d.scr.queue = reinterpret_cast<int *>(base + 20 * m);
+        d.scr.rq = reinterpret_cast<int *>(base + 24 * m);
         d.scr.dag = reinterpret_cast<unsigned char *>(base + 32 * m);
         {
             char *pb = base + ((((size_t)m + 16) * kScratchPerPoint + 255) & ~(size_t)255);
@@ -392,6 +391,8 @@ extern "C" int fdgpu_solve_device(fdgpu_ctx *ctx, int n, const fdgpu_station *st
             for (int j = 0; j < 6; j++) o.phase_cycles[j] = hst[k].phase_cycles[j];
             o.t_start_ns = hst[k].t_start_ns;
             o.t_end_ns = hst[k].t_end_ns;
+            o.pipelined_sweeps = hst[k].pipelined_sweeps;
+            o.detail = hst[k].status;
         }
         if (hst[k].status && rc == FDGPU_OK) rc = FDGPU_ESCHED;
     }

@@ -9,9 +9,9 @@
  * of their inner-layer neighbour (ties in fill order, src/sphfd.c:1024-1033 and glibc's stable
  * qsort); a point reads its eight in-face neighbours, seeing the new value of those already
  * updated and the old value of the others.  So the face is a DAG: an edge runs from each point to
- * every in-face neighbour with a larger key (time bits, fill index).  Walking it in Kahn rounds —
- * every point whose earlier neighbours are all done is evaluated in parallel, then releases its
- * later neighbours — reproduces the sequential order exactly.  No sort is needed.
+ * every in-face neighbour with a larger key (time bits, fill index).  Walking it in dependency order —
+ * every point whose earlier neighbours are all done may be evaluated, then releases its later
+ * neighbours — reproduces the sequential order exactly.  No sort is needed.
  *
  * The one sequential coupling that is not a neighbour relation is the stale (t0,t4) pair of
  * fdsph2d (src/sphfd.c:6116-6121): a point whose first 2-D trial comes before any 3-D / new-edge
@@ -20,7 +20,9 @@
  * done, and its pair is the record of the largest-key earlier point that made a writer call (or
  * the face's entry pair).  This is rare (hundreds of points per million).
  *
- * There are no spin-waits: CTAs synchronise only with __syncthreads, and every loop is bounded.
+ * Within a walk the warps of the CTA are independent workers that meet only at shared-memory
+ * counters (see "warp workers" below); every wait among them is bounded and ends in an error
+ * status, never in a hang.
  */
 #include <cuda_runtime.h>
 #include <math.h>
@@ -30,12 +32,14 @@
 #include "fdgpu_trials.cuh"
 #include "fdgpu_layout.h"
 
-#define FD_BLOCK 512
+#define FD_WARPS 12                 /* independent workers per station */
+#define FD_BLOCK (FD_WARPS * 32)
 
 /* optional per-phase cycle counters (thread 0, between barriers) for profiling builds */
 #ifdef FDGPU_PHASE_TIMERS
 #define FD_TIC(v) long long v = clock64()
-#define FD_TOC(k, v) do { if (threadIdx.x == 0) sh.cyc[k] += clock64() - (v); } while (0)
+#define FD_TOC(k, v) \
+    do { if ((threadIdx.x & 31) == 0) atomicAdd(reinterpret_cast<unsigned long long *>(&sh.cyc[k]), (unsigned long long)(clock64() - (v))); } while (0)
 #else
 #define FD_TIC(v) do { } while (0)
 #define FD_TOC(k, v) do { } while (0)
@@ -121,8 +125,9 @@ struct Shared {
     int radius, rad0, reverse, headpref;
     int headw[8];
     float carry_t0, carry_t4;
-    int cnt[2];
-    int ndef;
+    /* current walk: ready queue, queue of points waiting for an inherited stencil state, idle
+     * workers, finished nodes */
+    int qhead, qtail, qcap, rqhead, rqtail, rqcap, idle, ndone;
     unsigned long long exitkey;
     /* current face */
     int face, layer, ulo, uhi, vlo, vhi, nuf, n, n_pad;
@@ -137,8 +142,8 @@ struct Shared {
     int sweeps;
     int restart_wall[8];
     long long cyc[6];
-    /* plane-pipelined sweep: number of planes, layer of plane 0, queue tail, done flag */
-    int pipelined, np, player0, qtail;
+    /* plane-pipelined sweep: on/off, number of planes, layer of plane 0 */
+    int pipelined, np, player0;
     long long psweeps;
 };
 
@@ -202,10 +207,30 @@ struct Counters {
 };
 
 /* ---------------------------------------------------------------------------------------------- */
-/* trial-major rounds                                                                              */
+/* warp workers                                                                                    */
+/*                                                                                                 */
+/* A walk — one face, or one plane-pipelined sweep — is a dependency graph whose ready nodes sit   */
+/* in a queue.  Every warp of the CTA is an independent worker: it claims up to 32 ready nodes,     */
+/* evaluates them (one lane per node for the per-node steps, the stencil trials of all its nodes   */
+/* spread over the 32 lanes), commits them and queues the nodes they complete.  Warps meet only at */
+/* shared-memory counters, so the FP64 work of some warps hides the memory and control latency of  */
+/* the others, and a node starts as soon as its own inputs are final instead of at the next round. */
+/*                                                                                                 */
+/* Queue: positions are taken with an atomic on the tail and written after; every entry starts as */
+/* -1, so a worker that claimed a position not yet written waits for it (briefly: the writer is    */
+/* between two instructions).  Stores of a node's time and of its queue entries are ordered by     */
+/* __threadfence_block before the counters that publish them.                                     */
+/*                                                                                                 */
+/* Quiescence: a worker with nothing to claim counts itself idle.  When every worker is idle and   */
+/* the queue is empty and stays so (tail read before and after the idle count), no node is in      */
+/* flight and none can become ready; if points were put aside for an inherited stencil state, one  */
+/* worker (elected with a lock, the test repeated under it) resolves the first of them.  Every     */
+/* wait is bounded: a worker idle for FD_WAIT_CYCLES without progress sets the station's status    */
+/* and all workers leave the walk.                                                                  */
 
-#define FD_CHUNK 128   /* points per evaluation chunk */
-#define FD_TPP 4       /* threads per point in phase A */
+#define NB_PAD 19                    /* context row stride: the 32 rows fall on distinct banks */
+#define FD_WAIT_CYCLES (4ll << 30)   /* about 2 s at the maximum SM clock */
+#define FD_QSPIN (1 << 22)           /* polls of an unwritten queue entry before giving up */
 
 #define FD_DESC_ROW(F)                                                                              \
     make_desc<F>(0), make_desc<F>(1), make_desc<F>(2), make_desc<F>(3), make_desc<F>(4), make_desc<F>(5), \
@@ -215,40 +240,31 @@ struct Counters {
 __constant__ TrialDesc c_desc[FDN_NFACE * FDN_NTRIAL] = {FD_DESC_ROW(0), FD_DESC_ROW(1), FD_DESC_ROW(2),
                                                          FD_DESC_ROW(3), FD_DESC_ROW(4), FD_DESC_ROW(5)};
 
-/* item list regions by kind: 3-D, new-edge, 2-D, new-face, 1-D */
-__device__ __forceinline__ int item_off(int kind)
-{
-    return (kind == 0 ? 0 : kind == 1 ? 4 : kind == 2 ? 8 : kind == 3 ? 16 : 17) * FD_CHUNK;
-}
-
 __device__ __forceinline__ int kind_of(int K)
 {
     return K < TK_NE0 ? 0 : K < TK_2D0 ? 1 : K < TK_NF ? 2 : K < TK_1D0 ? 3 : 4;
 }
 
-struct Smem {
+/* shared by the CTA: the current face's trial descriptors */
+struct CtaSmem {
     TrialDesc desc[FDN_NTRIAL];
-    float t[FD_CHUNK][NB_N];
-    float s[FD_CHUNK][NB_N];
-    int idx[FD_CHUNK];               /* fill index of the chunk's point */
-    int lay[FD_CHUNK];               /* its face layer */
-    int pl[FD_CHUNK];                /* its plane in a pipelined sweep (-1 otherwise) */
-    int z[FD_CHUNK], y[FD_CHUNK];
-    unsigned guardm[FD_CHUNK];       /* trials whose guards pass (first-contact gates excluded) */
-    unsigned evalm[FD_CHUNK];        /* trials whose value was computed in the parallel phases */
-    double res[FD_CHUNK][FDN_NTRIAL];
-    double x2[FD_CHUNK][8];
-    unsigned short items[22 * FD_CHUNK];
-    int cnt[5];
 };
+constexpr int kCtaSmemBytes = (int)((sizeof(CtaSmem) + 15) & ~(size_t)15);
 
-/* dependency state of the current face: one in-degree byte per point (0xFF once done) and one
- * byte marking which of its 8 neighbours come earlier in sort order; in shared memory after Smem
- * when the face fits, else in the station's global scratch */
-__device__ __forceinline__ unsigned char *dag_indeg(const fd_station_dev &sd, Smem &sm, bool in_smem)
-{
-    return in_smem ? reinterpret_cast<unsigned char *>(&sm + 1) : sd.scr.dag;
-}
+/* one warp's chunk of up to 32 nodes; slot = lane of the node */
+struct WarpSmem {
+    double res[32][FDN_NTRIAL];            /* trial values (2-D: after the causality selection) */
+    float t[32][NB_PAD];                   /* 18-node time context */
+    float s[32][NB_PAD];                   /* 18-node slowness context */
+    float s0[32], s4[32];                  /* stencil state entering the 2-D block */
+    int z[32], y[32];                      /* grid z and y of the node */
+    unsigned short items[FDN_NTRIAL * 32]; /* (slot << 5 | trial) to evaluate, trial-major */
+};
+static_assert(sizeof(WarpSmem) % 16 == 0, "keeps the dependency bytes after the warp areas aligned");
+constexpr int kSmemBase = kCtaSmemBytes + FD_WARPS * (int)sizeof(WarpSmem);
+
+template <class T>
+__device__ __forceinline__ T vload(const T &x) { return *const_cast<const volatile T *>(&x); }
 
 __device__ __forceinline__ void nb_off(int k, int &du, int &dv)
 {
@@ -298,7 +314,7 @@ __device__ __forceinline__ bool guard_static(const float *t18, int u, int v, int
 }
 
 /* causality floor of trial K: the largest time among the slots its accepted value cannot be below
- * (2-D: its three own slots; the stale pair is added in the scan) */
+ * (2-D: its three own slots; the stale pair is added later) */
 template <int F, int K>
 __device__ __forceinline__ float floor_of(const float *t18)
 {
@@ -320,39 +336,6 @@ struct Rect {
     int u, v, nu, nv, ulo, uhi, vlo, vhi;
 };
 
-/* phase A2: thread q of a point handles trials K = q, q+4, ...: guards, pruning, items.  Corner
- * and edge trials are queued now; new-edge trials only when no corner trial can run (the
- * first-contact gate is then decided by the initial value); 2-D trials after the corners. */
-template <int F, int K>
-__device__ __forceinline__ void a2_trials(Smem &sm, int slot, const Rect &r, double g0, bool any3d, unsigned &gm,
-                                          unsigned &em)
-{
-    if constexpr (K < FDN_NTRIAL) {
-        constexpr fdn_trial tr = fd_face_trials[F][K];
-        const float *t18 = sm.t[slot];
-        if (guard_static<F, K>(t18, r.u, r.v, r.nu, r.nv, r.ulo, r.uhi, r.vlo, r.vhi)) {
-            gm |= 1u << K;
-            if constexpr (tr.kind == FDN_3D) {
-                if (!prunable(floor_of<F, K>(t18), g0)) em |= 1u << K;
-            } else if constexpr (tr.kind == FDN_1D) {
-                if (!(f2d(floor_of<F, K>(t18)) >= g0)) em |= 1u << K;
-            } else if constexpr (tr.kind == FDN_NE) {
-                if (!any3d && g0 > 1.0e9 && !prunable(floor_of<F, K>(t18), g0)) em |= 1u << K;
-            }
-        }
-        a2_trials<F, K + FD_TPP>(sm, slot, r, g0, any3d, gm, em);
-    }
-}
-
-template <int F>
-__device__ __forceinline__ bool any_corner(const float *t18, const Rect &r)
-{
-    return guard_static<F, 0>(t18, r.u, r.v, r.nu, r.nv, r.ulo, r.uhi, r.vlo, r.vhi)
-           || guard_static<F, 1>(t18, r.u, r.v, r.nu, r.nv, r.ulo, r.uhi, r.vlo, r.vhi)
-           || guard_static<F, 2>(t18, r.u, r.v, r.nu, r.nv, r.ulo, r.uhi, r.vlo, r.vhi)
-           || guard_static<F, 3>(t18, r.u, r.v, r.nu, r.nv, r.ulo, r.uhi, r.vlo, r.vhi);
-}
-
 __device__ __forceinline__ Rect rect_of(const Shared &sh, int i)
 {
     Rect r;
@@ -364,102 +347,148 @@ __device__ __forceinline__ Rect rect_of(const Shared &sh, int i)
 }
 
 template <int F>
-__device__ void phase_a2(Smem &sm, const Shared &sh, int slot, int q)
+__device__ __forceinline__ bool any_corner(const float *t18, const Rect &r)
 {
-    const int i = sm.idx[slot];
-    const Rect r = rect_of(sh, i);
-    const float *t18 = sm.t[slot];
-    const double g0 = f2d(t18[NB_POINT]);
-    const bool any3d = any_corner<F>(t18, r);
-    unsigned gm = 0, em = 0;
-    switch (q) {
-    case 0: a2_trials<F, 0>(sm, slot, r, g0, any3d, gm, em); break;
-    case 1: a2_trials<F, 1>(sm, slot, r, g0, any3d, gm, em); break;
-    case 2: a2_trials<F, 2>(sm, slot, r, g0, any3d, gm, em); break;
-    default: a2_trials<F, 3>(sm, slot, r, g0, any3d, gm, em); break;
-    }
-    if (gm) atomicOr(&sm.guardm[slot], gm);
-    if (em) atomicOr(&sm.evalm[slot], em);
-    unsigned m = em;
-    while (m) {
-        const int K = __ffs(m) - 1;
-        m &= m - 1;
-        const int kind = kind_of(K);
-        sm.items[item_off(kind) + atomicAdd(&sm.cnt[kind], 1)] = (unsigned short)((slot << 5) | K);
+    return guard_static<F, 0>(t18, r.u, r.v, r.nu, r.nv, r.ulo, r.uhi, r.vlo, r.vhi)
+           || guard_static<F, 1>(t18, r.u, r.v, r.nu, r.nv, r.ulo, r.uhi, r.vlo, r.vhi)
+           || guard_static<F, 2>(t18, r.u, r.v, r.nu, r.nv, r.ulo, r.uhi, r.vlo, r.vhi)
+           || guard_static<F, 3>(t18, r.u, r.v, r.nu, r.nv, r.ulo, r.uhi, r.vlo, r.vhi);
+}
+
+/* Guards, pruning and the trials to evaluate before the 2-D block: gm = trials whose guards pass
+ * (first-contact gates excluded), em = corner and 1-D trials that can lower the minimum, and
+ * new-edge trials when no corner can run (their gate is then decided by the initial value). */
+template <int F, int K>
+__device__ __forceinline__ void guard_trials(const float *t18, const Rect &r, double g0, bool any3d, unsigned &gm,
+                                             unsigned &em)
+{
+    if constexpr (K < FDN_NTRIAL) {
+        constexpr fdn_trial tr = fd_face_trials[F][K];
+        if (guard_static<F, K>(t18, r.u, r.v, r.nu, r.nv, r.ulo, r.uhi, r.vlo, r.vhi)) {
+            gm |= 1u << K;
+            if constexpr (tr.kind == FDN_3D) {
+                if (!prunable(floor_of<F, K>(t18), g0)) em |= 1u << K;
+            } else if constexpr (tr.kind == FDN_1D) {
+                if (!(f2d(floor_of<F, K>(t18)) >= g0)) em |= 1u << K;
+            } else if constexpr (tr.kind == FDN_NE) {
+                if (!any3d && g0 > 1.0e9 && !prunable(floor_of<F, K>(t18), g0)) em |= 1u << K;
+            }
+        }
+        guard_trials<F, K + 1>(t18, r, g0, any3d, gm, em);
     }
 }
 
-/* phase G: replay the corner and new-edge trials (all writers of the stencil state come before
- * the 2-D block) to get the running minimum entering the 2-D block — an upper bound for every
- * 2-D trial's turn — and the stale (t0,t4) those trials test against; queue the 2-D trials that
- * can still lower the minimum.  Thread q takes 2-D trials 8+q and 12+q. */
-__device__ void phase_g(Smem &sm, int slot, int q, float it0, float it4)
+template <int F>
+__device__ __forceinline__ void guards_face(const float *t18, const Rect &r, unsigned &gm, unsigned &em)
 {
-    const float *t18 = sm.t[slot];
-    const unsigned gm = sm.guardm[slot], em = sm.evalm[slot];
+    const double g0 = f2d(t18[NB_POINT]);
+    const bool any3d = any_corner<F>(t18, r);
+    gm = 0;
+    em = 0;
+    guard_trials<F, 0>(t18, r, g0, any3d, gm, em);
+}
+
+__device__ __forceinline__ void guards(int face, const float *t18, const Rect &r, unsigned &gm, unsigned &em)
+{
+    switch (face) {
+    case 0: guards_face<0>(t18, r, gm, em); break;
+    case 1: guards_face<1>(t18, r, gm, em); break;
+    case 2: guards_face<2>(t18, r, gm, em); break;
+    case 3: guards_face<3>(t18, r, gm, em); break;
+    case 4: guards_face<4>(t18, r, gm, em); break;
+    default: guards_face<5>(t18, r, gm, em); break;
+    }
+}
+
+/* append the items (lane, K) for K in [k0, k1) whose bit is set in the lane's em, trial-major */
+__device__ __forceinline__ int push_items(unsigned short *items, int n, unsigned em, int k0, int k1, int lane)
+{
+    const unsigned below = (1u << lane) - 1u;
+    for (int K = k0; K < k1; K++) {
+        const bool on = (em >> K) & 1u;
+        const unsigned b = __ballot_sync(0xffffffffu, on);
+        if (on) items[n + __popc(b & below)] = (unsigned short)((lane << 5) | K);
+        n += __popc(b);
+    }
+    return n;
+}
+
+/* evaluate items[0..n) with the warp's lanes; a 2-D value is stored after the causality selection
+ * against its floor, which includes the stencil state entering the 2-D block (src/sphfd.c:6116-6121) */
+__device__ void eval_items(const fd_station_dev &sd, const CtaSmem &cs, WarpSmem &ws, int n, int lane, Counters &cn)
+{
+    for (int j = lane; j < n; j += 32) {
+        const unsigned it = ws.items[j];
+        const int slot = (int)(it >> 5), K = (int)(it & 31);
+        const TrialDesc &d = cs.desc[K];
+        const int z = ws.z[slot], y = ws.y[slot];
+        const float *t18 = ws.t[slot], *s18 = ws.s[slot];
+        const int kind = kind_of(K);
+        double v;
+        switch (kind) {
+        case 0: v = eval_3d(d, t18, s18, sd.g, z, y); break;
+        case 1: v = eval_ne(d, t18, s18, sd.g, z, y); break;
+        case 2: {
+            double x1, x2;
+            eval_2d(d, t18, s18, sd.g, z, y, x1, x2);
+            if (x1 != x1) {
+                v = 1.e11;
+            } else {
+                const float fl = fmaxf(fmaxf(fmaxf(t18[d.slot[1]], t18[d.slot[2]]), fmaxf(t18[d.slot[3]], ws.s0[slot])),
+                                       ws.s4[slot]);
+                const double f = f2d(fl);
+                const bool bad1 = lt(x1, f), bad2 = lt(x2, f);
+                v = bad1 ? (bad2 ? 1.e11 : x2) : (bad2 ? x1 : (lt(x2, x1) ? x2 : x1));
+            }
+            break;
+        }
+        case 3: v = eval_nf(d, t18, s18, sd.g, z, y); break;
+        default: v = eval_1d(d, t18, s18, sd.g, z, y); break;
+        }
+        ws.res[slot][K] = v;
+        cn.n[kind]++;
+    }
+}
+
+/* Replay of the corner and new-edge trials (every writer of the stencil state comes before the
+ * 2-D block): the running minimum entering the 2-D block — an upper bound for every 2-D trial's
+ * turn — and the stale (t0,t4) those trials test against.  Returns the 2-D trials that can still
+ * lower the minimum. */
+__device__ unsigned stale_pair(const CtaSmem &cs, WarpSmem &ws, int slot, unsigned gm, unsigned em, float it0,
+                               float it4)
+{
+    const float *t18 = ws.t[slot];
     double g1 = f2d(t18[NB_POINT]);
     float s0 = it0, s4 = it4;
     for (int K = 0; K < TK_NE0; K++) {
         if (!((gm >> K) & 1u)) continue;
-        s0 = t18[sm.desc[K].slot[0]];
-        s4 = t18[sm.desc[K].slot[4]];
+        s0 = t18[cs.desc[K].slot[0]];
+        s4 = t18[cs.desc[K].slot[4]];
         if ((em >> K) & 1u) {
-            const double v = sm.res[slot][K];
+            const double v = ws.res[slot][K];
             if (lt(v, g1)) g1 = v;
         }
     }
     const bool gate = lt(1.0e9, g1);
     for (int K = TK_NE0; K < TK_2D0; K++) {
         if (!gate || !((gm >> K) & 1u)) continue;
-        s0 = t18[sm.desc[K].slot[0]];
-        s4 = t18[sm.desc[K].slot[4]];
+        s0 = t18[cs.desc[K].slot[0]];
+        s4 = t18[cs.desc[K].slot[4]];
         if ((em >> K) & 1u) {
-            const double v = sm.res[slot][K];
+            const double v = ws.res[slot][K];
             if (lt(v, g1)) g1 = v;
         }
     }
+    ws.s0[slot] = s0;
+    ws.s4[slot] = s4;
     unsigned add = 0;
-    for (int K = TK_2D0 + q; K < TK_NF; K += FD_TPP) {
+    for (int K = TK_2D0; K < TK_NF; K++) {
         if (!((gm >> K) & 1u)) continue;
-        const TrialDesc &d = sm.desc[K];
+        const TrialDesc &d = cs.desc[K];
         const float fl = fmaxf(fmaxf(fmaxf(t18[d.slot[1]], t18[d.slot[2]]), fmaxf(t18[d.slot[3]], s0)), s4);
-        if (prunable(fl, g1)) continue;
-        add |= 1u << K;
-        sm.items[item_off(2) + atomicAdd(&sm.cnt[2], 1)] = (unsigned short)((slot << 5) | K);
+        if (!prunable(fl, g1)) add |= 1u << K;
     }
-    if (add) atomicOr(&sm.evalm[slot], add);
-}
-
-/* evaluate queued items of kinds [k0, k1] with all threads */
-__device__ void run_items(const fd_station_dev &sd, Smem &sm, int k0, int k1, Counters &cn)
-{
-    int start[6];
-    start[0] = 0;
-    for (int k = 0; k < 5; k++) start[k + 1] = start[k] + ((k >= k0 && k <= k1) ? sm.cnt[k] : 0);
-    const int total = start[5];
-    for (int j = threadIdx.x; j < total; j += blockDim.x) {
-        int kind = 0;
-        while (j >= start[kind + 1]) kind++;
-        const unsigned it = sm.items[item_off(kind) + (j - start[kind])];
-        const int slot = (int)(it >> 5), K = (int)(it & 31);
-        const TrialDesc &d = sm.desc[K];
-        const int z = sm.z[slot], y = sm.y[slot];
-        const float *t18 = sm.t[slot], *s18 = sm.s[slot];
-        switch (kind) {
-        case 0: sm.res[slot][K] = eval_3d(d, t18, s18, sd.g, z, y); break;
-        case 1: sm.res[slot][K] = eval_ne(d, t18, s18, sd.g, z, y); break;
-        case 2: {
-            double x1, x2;
-            eval_2d(d, t18, s18, sd.g, z, y, x1, x2);
-            sm.res[slot][K] = x1;
-            sm.x2[slot][K - TK_2D0] = x2;
-            break;
-        }
-        case 3: sm.res[slot][K] = eval_nf(d, t18, s18, sd.g, z, y); break;
-        default: sm.res[slot][K] = eval_1d(d, t18, s18, sd.g, z, y); break;
-        }
-        cn.n[kind]++;
-    }
+    return add;
 }
 
 /* ---------------------------------------------------------------------------------------------- */
@@ -490,7 +519,7 @@ __device__ unsigned earlier_mask(const fd_station_dev &sd, const Shared &sh, int
         xyz[fr.axis_u] = sh.ulo + ju;
         xyz[fr.axis_v] = sh.vlo + jv;
         xyz[fr.axis_n] = inner_layer;
-        return sd.T[((long long)xyz[2] * sd.g.ny + xyz[1]) * sd.g.nx + xyz[0]];
+        return vload(sd.T[((long long)xyz[2] * sd.g.ny + xyz[1]) * sd.g.nx + xyz[0]]);
     };
     const unsigned long long ki = node_key(tin(iu, iv), i);
     unsigned em = 0;
@@ -505,21 +534,35 @@ __device__ unsigned earlier_mask(const fd_station_dev &sd, const Shared &sh, int
     return em;
 }
 
+/* append e to a queue with tail counter `tail`; a position past the capacity (a node queued more
+ * often than the walk allows) is refused */
+__device__ __forceinline__ void enqueue_to(int *queue, int &tail, int cap, Shared &sh, int e)
+{
+    const int pos = atomicAdd(&tail, 1);
+    if (pos < cap)
+        queue[pos] = e;
+    else
+        atomicCAS(&sh.status, 0, 10);
+}
+
+__device__ __forceinline__ void enqueue(int *queue, Shared &sh, int e) { enqueue_to(queue, sh.qtail, sh.qcap, sh, e); }
+
 /* node (plane pp, fill index i) is final: record (last plane), release its later in-plane
  * neighbours and the plane pp+1 nodes whose inner block contains it */
-__device__ void pipelined_release(const fd_station_dev &sd, Shared &sh, int slot, int i, int pp, bool writer,
-                                  float st0, float st4, const float *t18)
+__device__ void pipelined_release(const fd_station_dev &sd, Shared &sh, int i, int pp, bool writer, float st0,
+                                  float st4, float tin)
 {
     const int nplane = sh.n, nvf = sh.n / sh.nuf, iu = i % sh.nuf, iv = i / sh.nuf;
     const fdn_frame fr = frame_of(sh.face);
     if (pp == sh.np - 1) {
         if (writer) {
             sd.scr.rec[i] = make_float2(st0, st4);
-            atomicMax(&sh.exitkey, node_key(t18[13], i));
+            atomicMax(&sh.exitkey, node_key(tin, i));
         } else {
             sd.scr.rec[i] = make_float2(__int_as_float(0x7fc00000), __int_as_float(0x7fc00000));
         }
     }
+    __threadfence_block();
     const long long base = (long long)pp * nplane;
     unsigned later = inrect_mask(iu, iv, sh.nuf, nvf) & ~(unsigned)sd.scr.pemask[base + i];
     while (later) {
@@ -529,7 +572,7 @@ __device__ void pipelined_release(const fd_station_dev &sd, Shared &sh, int slot
         nb_off(k, du, dv);
         const int j = (iv + dv) * sh.nuf + iu + du;
         const unsigned old = atomicSub(&sd.scr.pcount[base + j], 1u << 8);
-        if (old == (1u << 8)) sd.scr.pqueue[atomicAdd(&sh.qtail, 1)] = (int)(base + j);
+        if (old == (1u << 8)) enqueue(sd.scr.pqueue, sh, (int)(base + j));
     }
     if (pp + 1 < sh.np) {
         const long long nb = base + nplane;
@@ -544,112 +587,31 @@ __device__ void pipelined_release(const fd_station_dev &sd, Shared &sh, int slot
                 /* inner block of node j complete: its in-plane order is now known */
                 const unsigned em = earlier_mask(sd, sh, j, layer);
                 sd.scr.pemask[nb + j] = (unsigned char)em;
+                __threadfence_block();
                 const unsigned lat = (unsigned)__popc(inrect_mask(ju, jv, sh.nuf, nvf) & ~em);
                 const unsigned w = old - 1u;
                 const unsigned prev = lat ? atomicSub(&sd.scr.pcount[nb + j], lat << 8) : w;
-                if (prev - (lat << 8) == 0u) sd.scr.pqueue[atomicAdd(&sh.qtail, 1)] = (int)(nb + j);
+                if (prev - (lat << 8) == 0u) enqueue(sd.scr.pqueue, sh, (int)(nb + j));
             }
     }
 }
 
-/* Phase C for one point: the reference's sequential minimum over the 22 trials, from the values
- * computed in the parallel phases (new-edge and new-face values that were not precomputed are
- * evaluated here — they are needed only at first contact), then the commit
- * (src/sphfd.c:1756-1760), the point's stencil-state record and the release of its later
- * neighbours into list `out`.  Returns false if the point must wait for an inherited state. */
-__device__ bool phase_c(const fd_station_dev &sd, Shared &sh, Smem &sm, int slot, bool have_inherit, float it0,
-                        float it4, int out, unsigned char *dag, Counters &cn)
+/* face walk: node i is final; mark it done and release its later in-face neighbours */
+__device__ void face_release(const fd_station_dev &sd, Shared &sh, unsigned char *dag, int i, bool writer,
+                             float st0, float st4)
 {
-    const int i = sm.idx[slot];
-    const float *t18 = sm.t[slot], *s18 = sm.s[slot];
-    const unsigned gm = sm.guardm[slot], em = sm.evalm[slot];
-    const double told = f2d(t18[NB_POINT]);
-    /* a 2-D trial before any corner / new-edge call would read the previous point's t0,t4 */
-    if (!have_inherit && (gm & 0xFu) == 0 && !((gm & 0xF0u) && told > 1.0e9) && (gm & 0xFF00u)) {
-        if (sh.pipelined) sh.status = 6;   /* excluded by the pipelining precondition */
-        return false;
-    }
-    const int z = sm.z[slot], y = sm.y[slot];
-    double guess = told;
-    float st0 = it0, st4 = it4;
-    int writers = 0;
-    bool gate = false;
-    int lastK = -1;
-    double last_gb = 0.0, last_v = 0.0;
-#pragma unroll 1
-    for (int K = 0; K < FDN_NTRIAL; K++) {
-        /* the first-contact tests are made on entry to their blocks (src/sphfd.c:1375, :1698) */
-        if (K == TK_NE0 || K == TK_NF) gate = lt(1.0e9, guess);
-        if (!((gm >> K) & 1u)) continue;
-        const TrialDesc &d = sm.desc[K];
-        const bool ev = (em >> K) & 1u;
-        double v;
-        if (K < TK_2D0 || K == TK_NF) {
-            /* corner, new-edge, new-face: writers of the stencil state */
-            if (K >= TK_NE0 && !gate) continue;
-            st0 = t18[d.slot[0]];
-            st4 = t18[d.slot[4]];
-            writers++;
-            if (ev) {
-                v = sm.res[slot][K];
-            } else if (K >= TK_NE0) {
-                /* new-edge / new-face value not precomputed: evaluate unless it cannot improve */
-                float fl = t18[d.slot[0]];
-                for (int k = 1; k < 5; k++) fl = fmaxf(fl, t18[d.slot[k]]);
-                if (prunable(fl, guess)) continue;
-                v = (K == TK_NF) ? eval_nf(d, t18, s18, sd.g, z, y) : eval_ne(d, t18, s18, sd.g, z, y);
-                cn.n[K == TK_NF ? 3 : 1]++;
-            } else {
-                continue;
-            }
-        } else if (K < TK_NF) {
-            /* 2-D: the causality floor includes the stale t0,t4 */
-            if (!ev) continue;
-            const float fl = fmaxf(fmaxf(fmaxf(t18[d.slot[1]], t18[d.slot[2]]), fmaxf(t18[d.slot[3]], st0)), st4);
-            const double x1 = sm.res[slot][K], x2 = sm.x2[slot][K - TK_2D0];
-            if (x1 != x1) {
-                v = 1.e11;
-            } else {
-                const double f = f2d(fl);
-                const bool bad1 = lt(x1, f), bad2 = lt(x2, f);
-                v = bad1 ? (bad2 ? 1.e11 : x2) : (bad2 ? x1 : (lt(x2, x1) ? x2 : x1));
-            }
-        } else {
-            if (!ev) continue;
-            v = sm.res[slot][K];
-        }
-        if (lt(v, guess)) {
-            if (d.head) { lastK = K; last_gb = guess; last_v = v; }
-            guess = v;
-        }
-    }
-    if (lt(guess, told)) {
-        const fdn_frame fr = frame_of(sh.face);
-        int xyz[3];
-        xyz[fr.axis_u] = sh.ulo + i % sh.nuf;
-        xyz[fr.axis_v] = sh.vlo + i / sh.nuf;
-        xyz[fr.axis_n] = sm.lay[slot];
-        const long long pT = ((long long)xyz[2] * sd.g.ny + xyz[1]) * sd.g.nx + xyz[0];
-        sd.T[pT] = __double2float_rn(guess);
-        if (lastK >= 0) {
-            /* only the last head trial that lowered the minimum sets the measure that is tested */
-            const double fhead = (last_gb - last_v) / head_den(sm.desc[lastK], s18, sd.g, z, y);
-            if (fhead > FD_HEADTEST) atomicAdd(&sh.headw[fr.headw], 1);
-        }
-    }
-    if (sh.pipelined) {
-        pipelined_release(sd, sh, slot, i, sm.pl[slot], writers != 0, st0, st4, t18);
-        return true;
-    }
-    if (writers) {
+    if (writer) {
         sd.scr.rec[i] = make_float2(st0, st4);
         atomicMax(&sh.exitkey, sd.scr.key[i]);
     } else {
         sd.scr.rec[i] = make_float2(__int_as_float(0x7fc00000), __int_as_float(0x7fc00000));
     }
-    /* done; release the later in-face neighbours */
+    __threadfence_block();
+    /* done; a point waiting for the stencil state left before it resumes its search */
+    const int waiter = atomicExch(&sd.scr.pst[i], -2);
+    if (waiter >= 0) enqueue_to(sd.scr.rq, sh.rqtail, sh.rqcap, sh, waiter);
     const int nvf = sh.n / sh.nuf, iu = i % sh.nuf, iv = i / sh.nuf;
-    unsigned char *emask = dag + sh.n_pad;
+    const unsigned char *emask = dag + sh.n_pad;
     unsigned later = inrect_mask(iu, iv, sh.nuf, nvf) & ~(unsigned)emask[i];
     atomicOr(reinterpret_cast<unsigned *>(dag) + (i >> 2), 0xFFu << ((i & 3) * 8));
     while (later) {
@@ -660,104 +622,361 @@ __device__ bool phase_c(const fd_station_dev &sd, Shared &sh, Smem &sm, int slot
         const int j = (iv + dv) * sh.nuf + iu + du;
         const unsigned sh8 = (j & 3) * 8;
         const unsigned old = atomicSub(reinterpret_cast<unsigned *>(dag) + (j >> 2), 1u << sh8);
-        if (((old >> sh8) & 0xFFu) == 1u) sd.scr.wl[out][atomicAdd(&sh.cnt[out], 1)] = j;
+        if (((old >> sh8) & 0xFFu) == 1u) enqueue(sd.scr.queue, sh, j);
     }
+}
+
+/* The reference's sequential minimum over the 22 trials of one node, from the values computed
+ * by the warp (new-edge and new-face values that were not precomputed are evaluated here — they
+ * are needed only at first contact), then the commit (src/sphfd.c:1756-1760), the node's
+ * stencil-state record and the release of the nodes that wait on it.
+ *
+ * `permissive`: the node makes no writer call before its 2-D trials, so those test against a
+ * stencil state left by an earlier point; their values were computed with no stale floor.  A
+ * stale floor can only turn a 2-D value into the rejection value, so if no 2-D value lowered
+ * the running minimum the result is the one the true state gives and the node commits; else it
+ * returns false without committing. */
+__device__ bool commit_node(const fd_station_dev &sd, Shared &sh, const CtaSmem &cs, WarpSmem &ws, int slot, int i,
+                            int pp, long long pT, unsigned gm, unsigned em, float it0, float it4, bool permissive,
+                            unsigned char *dag, Counters &cn)
+{
+    const float *t18 = ws.t[slot], *s18 = ws.s[slot];
+    const double told = f2d(t18[NB_POINT]);
+    const int z = ws.z[slot], y = ws.y[slot];
+    double guess = told;
+    float st0 = it0, st4 = it4;
+    int writers = 0;
+    bool gate = false, win2d = false;
+    int lastK = -1;
+    double last_gb = 0.0, last_v = 0.0;
+#pragma unroll 1
+    for (int K = 0; K < FDN_NTRIAL; K++) {
+        /* the first-contact tests are made on entry to their blocks (src/sphfd.c:1375, :1698) */
+        if (K == TK_NE0 || K == TK_NF) gate = lt(1.0e9, guess);
+        if (!((gm >> K) & 1u)) continue;
+        const TrialDesc &d = cs.desc[K];
+        const bool ev = (em >> K) & 1u;
+        double v;
+        if (K < TK_2D0 || K == TK_NF) {
+            /* corner, new-edge, new-face: writers of the stencil state */
+            if (K >= TK_NE0 && !gate) continue;
+            st0 = t18[d.slot[0]];
+            st4 = t18[d.slot[4]];
+            writers++;
+            if (ev) {
+                v = ws.res[slot][K];
+            } else if (K >= TK_NE0) {
+                /* new-edge / new-face value not precomputed: evaluate unless it cannot improve */
+                float fl = t18[d.slot[0]];
+                for (int k = 1; k < 5; k++) fl = fmaxf(fl, t18[d.slot[k]]);
+                if (prunable(fl, guess)) continue;
+                v = (K == TK_NF) ? eval_nf(d, t18, s18, sd.g, z, y) : eval_ne(d, t18, s18, sd.g, z, y);
+                cn.n[K == TK_NF ? 3 : 1]++;
+            } else {
+                continue;
+            }
+        } else {
+            if (!ev) continue;
+            v = ws.res[slot][K];
+            if (K < TK_NF && lt(v, guess)) win2d = true;
+        }
+        if (lt(v, guess)) {
+            if (d.head) { lastK = K; last_gb = guess; last_v = v; }
+            guess = v;
+        }
+    }
+    if (permissive && win2d) return false;
+    if (lt(guess, told)) {
+        sd.T[pT] = __double2float_rn(guess);
+        if (lastK >= 0) {
+            /* only the last head trial that lowered the minimum sets the measure that is tested */
+            const double fhead = (last_gb - last_v) / head_den(cs.desc[lastK], s18, sd.g, z, y);
+            if (fhead > FD_HEADTEST) atomicAdd(&sh.headw[frame_of(sh.face).headw], 1);
+        }
+    }
+    if (sh.pipelined)
+        pipelined_release(sd, sh, i, pp, writers != 0, st0, st4, t18[13]);
+    else
+        face_release(sd, sh, dag, i, writers != 0, st0, st4);
     return true;
 }
 
-__device__ __forceinline__ void phase_a2_dispatch(Smem &sm, const Shared &sh, int slot, int q)
+/* Evaluate and commit one chunk: lane l holds queue entry e (-1 for none).  A node given with
+ * have_inherit uses (it0, it4) as the stencil state entering it.  All 32 lanes call. */
+__device__ void warp_chunk(const fd_station_dev &sd, Shared &sh, const CtaSmem &cs, WarpSmem &ws, int e,
+                           bool have_inherit, float it0, float it4, unsigned char *dag, Counters &cn)
 {
-    switch (sh.face) {
-    case 0: phase_a2<0>(sm, sh, slot, q); break;
-    case 1: phase_a2<1>(sm, sh, slot, q); break;
-    case 2: phase_a2<2>(sm, sh, slot, q); break;
-    case 3: phase_a2<3>(sm, sh, slot, q); break;
-    case 4: phase_a2<4>(sm, sh, slot, q); break;
-    default: phase_a2<5>(sm, sh, slot, q); break;
-    }
-}
-
-/* Evaluate points list[0..m) (m <= FD_CHUNK).  All threads call this. */
-__device__ void run_chunk(const fd_station_dev &sd, Shared &sh, Smem &sm, const int *list, int m, bool have_inherit,
-                          float it0, float it4, int out, unsigned char *dag, Counters &cn)
-{
-    const int tid = threadIdx.x;
-    if (tid < 5) sm.cnt[tid] = 0;
-    FD_TIC(ta);
-    /* A1: the 18-node context of each point, FD_TPP threads per point */
+    const int lane = threadIdx.x & 31;
+    const bool valid = e >= 0;
     const fdn_frame fr = frame_of(sh.face);
-    for (int r = tid; r < m * FD_TPP; r += blockDim.x) {
-        const int slot = r / FD_TPP, q = r % FD_TPP;
-        /* list entries: fill indices, or plane*n + fill index in a pipelined sweep */
-        const int e = list[slot];
-        const int pp = sh.pipelined ? e / sh.n : -1;
-        const int i = sh.pipelined ? e - pp * sh.n : e;
-        const int layer = sh.pipelined ? sh.player0 - pp * fr.inner : sh.layer;
+    int i = 0, pp = -1;
+    long long pT = 0;
+    unsigned gm = 0, em = 0;
+    bool permissive = false;
+    FD_TIC(ta);
+    if (valid) {
+        /* entries: fill indices, or plane * n + fill index in a pipelined sweep */
+        int layer = sh.layer;
+        if (sh.pipelined) {
+            pp = e / sh.n;
+            i = e - pp * sh.n;
+            layer = sh.player0 - pp * fr.inner;
+        } else {
+            i = e;
+        }
         const int u = sh.ulo + i % sh.nuf, v = sh.vlo + i / sh.nuf;
         int xyz[3];
         xyz[fr.axis_u] = u;
         xyz[fr.axis_v] = v;
         xyz[fr.axis_n] = layer;
-        const long long pT = ((long long)xyz[2] * sd.g.ny + xyz[1]) * sd.g.nx + xyz[0];
+        pT = ((long long)xyz[2] * sd.g.ny + xyz[1]) * sd.g.nx + xyz[0];
         const long long pS = (long long)xyz[2] * sd.s_sz + (long long)xyz[1] * sd.s_sy + xyz[0];
-        if (q == 0) {
-            sm.idx[slot] = i;
-            sm.lay[slot] = layer;
-            sm.pl[slot] = pp;
-            sm.z[slot] = xyz[2];
-            sm.y[slot] = xyz[1];
-            sm.guardm[slot] = 0;
-            sm.evalm[slot] = 0;
-        }
-        for (int nb = q; nb < NB_N; nb += FD_TPP) {
+        ws.z[lane] = xyz[2];
+        ws.y[lane] = xyz[1];
+        float *tr = ws.t[lane], *sr = ws.s[lane];
+        const long long inner_t = (long long)fr.inner * sh.sn, inner_s = (long long)fr.inner * sh.ssn;
+#pragma unroll
+        for (int nb = 0; nb < NB_N; nb++) {
             const int w = nb / 9, dv = (nb / 3) % 3 - 1, du = nb % 3 - 1;
             const int uu = u + du, vv = v + dv;
             float tv = 0.f, svv = 0.f;
             if (uu >= 0 && uu < sh.nu && vv >= 0 && vv < sh.nv) {
-                const long long off_n = (long long)(w * fr.inner);
-                tv = sd.T[pT + du * sh.su + dv * sh.sv + off_n * sh.sn];
-                svv = __ldg(&sd.S[pS + du * sh.ssu + dv * sh.ssv + off_n * sh.ssn]);
+                tv = sd.T[pT + du * sh.su + dv * sh.sv + (w ? inner_t : 0ll)];
+                svv = __ldg(&sd.S[pS + du * sh.ssu + dv * sh.ssv + (w ? inner_s : 0ll)]);
             }
-            sm.t[slot][nb] = tv;
-            sm.s[slot][nb] = svv;
+            tr[nb] = tv;
+            sr[nb] = svv;
         }
+        guards(sh.face, tr, rect_of(sh, i), gm, em);
+        /* a 2-D trial before any corner / new-edge call reads the state an earlier point left */
+        const double told = f2d(tr[NB_POINT]);
+        permissive = !have_inherit && (gm & 0xFu) == 0 && !((gm & 0xF0u) && told > 1.0e9) && (gm & 0xFF00u);
     }
-    __syncthreads();
-    /* A2: guards, pruning, corner / edge / first-contact items */
-    for (int r = tid; r < m * FD_TPP; r += blockDim.x) phase_a2_dispatch(sm, sh, r / FD_TPP, r % FD_TPP);
-    __syncthreads();
+    __syncwarp();
+    int n1 = push_items(ws.items, 0, em, TK_3D0, TK_2D0, lane);
+    n1 = push_items(ws.items, n1, em, TK_1D0, FDN_NTRIAL, lane);
+    __syncwarp();
     FD_TOC(1, ta);
     FD_TIC(tb);
-    run_items(sd, sm, 0, 4, cn);   /* corner, new-edge, 1-D (2-D not queued yet, new-face never) */
-    __syncthreads();
-    if (tid < 5) sm.cnt[tid] = 0;
-    __syncthreads();
-    for (int r = tid; r < m * FD_TPP; r += blockDim.x) phase_g(sm, r / FD_TPP, r % FD_TPP, it0, it4);
-    __syncthreads();
-    run_items(sd, sm, 2, 2, cn);
-    __syncthreads();
+    eval_items(sd, cs, ws, n1, lane, cn);
+    __syncwarp();
+    const float lo = __int_as_float(0xff800000);   /* -inf: no stale floor */
+    const float p0 = permissive ? lo : it0, p4 = permissive ? lo : it4;
+    if (valid) em |= stale_pair(cs, ws, lane, gm, em, p0, p4);
+    __syncwarp();
+    const int n2 = push_items(ws.items, 0, em, TK_2D0, TK_NF, lane);
+    __syncwarp();
+    eval_items(sd, cs, ws, n2, lane, cn);
+    __syncwarp();
     FD_TOC(2, tb);
     FD_TIC(tc);
-    if (tid < m) {
-        if (!phase_c(sd, sh, sm, tid, have_inherit, it0, it4, out, dag, cn))
-            sd.scr.deferred[atomicAdd(&sh.ndef, 1)] = list[tid];
+    bool fin = false;
+    if (valid) {
+        fin = commit_node(sd, sh, cs, ws, lane, i, pp, pT, gm, em, p0, p4, permissive, dag, cn);
+        if (!fin) {
+            if (sh.pipelined) {
+                atomicCAS(&sh.status, 0, 6);   /* excluded by the pipelining precondition */
+            } else {
+                atomicAdd(reinterpret_cast<unsigned long long *>(&sh.deferred), 1ull);
+                enqueue_to(sd.scr.rq, sh.rqtail, sh.rqcap, sh, e);
+            }
+        }
     }
-    __syncthreads();
+    const unsigned done = __ballot_sync(0xffffffffu, fin);
+    if (lane == 0 && done) {
+        __threadfence_block();
+        atomicAdd(&sh.ndone, __popc(done));
+    }
+    __syncwarp();
     FD_TOC(3, tc);
 }
 
+__device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long x)
+{
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long y = __shfl_xor_sync(0xffffffffu, x, o);
+        x = y > x ? y : x;
+    }
+    return x;
+}
+
+/* the face point that precedes point c in sort order (largest key below c's), -1 if none */
+__device__ int predecessor(const fd_station_dev &sd, int n, int c, int lane)
+{
+    const unsigned long long kc = sd.scr.key[c];
+    unsigned long long best = 0ull;   /* every key is above 0: times are not negative */
+    int j = lane;
+    for (; j + 96 < n; j += 128) {
+        const unsigned long long k0 = sd.scr.key[j], k1 = sd.scr.key[j + 32];
+        const unsigned long long k2 = sd.scr.key[j + 64], k3 = sd.scr.key[j + 96];
+        if (k0 < kc && k0 > best) best = k0;
+        if (k1 < kc && k1 > best) best = k1;
+        if (k2 < kc && k2 > best) best = k2;
+        if (k3 < kc && k3 > best) best = k3;
+    }
+    for (; j < n; j += 32) {
+        const unsigned long long k = sd.scr.key[j];
+        if (k < kc && k > best) best = k;
+    }
+    best = warp_max_u64(best);
+    return best ? (int)(best & 0xffffffffu) : -1;
+}
+
+/* Point w needs the stencil state left by the last point before it in sort order that made a
+ * writer call.  Walk back through the sort order: a done writer gives its record; a done
+ * non-writer passes the search to its predecessor; a point not yet done takes w as its waiter and
+ * queues it again when it finishes (a point has at most one waiter: waiters lie between it and the
+ * next pending point).  Before the face's first point the state is the one the face started with.
+ * Keys fall along the walk, so waits cannot form a cycle.  One warp; evaluates w when found. */
+__device__ void resume_waiter(const fd_station_dev &sd, Shared &sh, const CtaSmem &cs, WarpSmem &ws, int w,
+                              unsigned char *dag, Counters &cn)
+{
+    const int lane = threadIdx.x & 31;
+    int c = w;
+    for (int guard = 0; guard <= 2 * sh.n + 2; guard++) {
+        const int p = predecessor(sd, sh.n, c, lane);
+        int verdict = 0;   /* 0 continue from p, 1 found (t0,t4), 2 waiting, 3 retry p */
+        float t0 = sh.carry_t0, t4 = sh.carry_t4;
+        if (lane == 0) {
+            if (p < 0) {
+                verdict = 1;
+            } else {
+                int st = vload(sd.scr.pst[p]);
+                if (st != -2) {
+                    const int old = atomicCAS(&sd.scr.pst[p], -1, w);
+                    if (old == -1) verdict = 2;
+                    else if (old == -2) verdict = 3;
+                    else { atomicCAS(&sh.status, 0, 11); verdict = 2; }   /* a second waiter */
+                    st = old;
+                }
+                if (verdict == 0 || verdict == 3) {
+                    __threadfence_block();
+                    const float r0 = vload(sd.scr.rec[p].x), r4 = vload(sd.scr.rec[p].y);
+                    if (!isnan(r0)) { verdict = 1; t0 = r0; t4 = r4; }
+                    else verdict = 0;
+                }
+            }
+        }
+        verdict = __shfl_sync(0xffffffffu, verdict, 0);
+        if (verdict == 2) return;
+        if (verdict == 1) {
+            t0 = __shfl_sync(0xffffffffu, t0, 0);
+            t4 = __shfl_sync(0xffffffffu, t4, 0);
+            warp_chunk(sd, sh, cs, ws, lane == 0 ? w : -1, true, t0, t4, dag, cn);
+            return;
+        }
+        c = p;
+    }
+    if (lane == 0) atomicCAS(&sh.status, 0, 12);
+}
+
+/* nothing queued, every worker idle, and both queues unchanged across the idle count (lane 0) */
+__device__ __forceinline__ bool quiescent(Shared &sh)
+{
+    const int t0 = vload(sh.qtail), h0 = vload(sh.qhead), r0 = vload(sh.rqtail), g0 = vload(sh.rqhead);
+    if (h0 != t0 || r0 != g0) return false;
+    __threadfence_block();
+    if (vload(sh.idle) != FD_WARPS) return false;
+    __threadfence_block();
+    return vload(sh.qtail) == t0 && vload(sh.qhead) == t0 && vload(sh.rqtail) == r0 && vload(sh.rqhead) == r0;
+}
+
+/* claim one entry of a queue (lane 0): spins briefly for an entry whose writer is between its two
+ * instructions; -1 and a status on failure */
+__device__ __forceinline__ int read_entry(const int *queue, int pos, Shared &sh)
+{
+    const volatile int *q = queue + pos;
+    int e = *q;
+    for (int spin = 0; e < 0 && spin < FD_QSPIN; spin++) {
+        __nanosleep(32);
+        e = *q;
+    }
+    if (e < 0) atomicCAS(&sh.status, 0, 9);   /* a claimed entry never written */
+    return e;
+}
+
+/* the worker loop of one walk over `total` nodes; all warps call it between two CTA barriers */
+__device__ void run_walk(const fd_station_dev &sd, Shared &sh, const CtaSmem &cs, WarpSmem &ws, int *queue,
+                         int total, unsigned char *dag, Counters &cn)
+{
+    const int lane = threadIdx.x & 31;
+    bool idle = false;
+    long long since = clock64();
+    long long chunks = 0;
+    for (;;) {
+        int act = 0, h = 0, m = 0;   /* act: 0 wait, 1 chunk, 2 resume a waiter, 3 leave */
+        if (lane == 0) {
+            if (vload(sh.status) != 0 || vload(sh.ndone) >= total) {
+                act = 3;
+            } else {
+                const int rh = vload(sh.rqhead), rt0 = vload(sh.rqtail), rt = rt0 < sh.rqcap ? rt0 : sh.rqcap;
+                const int head = vload(sh.qhead), qt = vload(sh.qtail), tail = qt < sh.qcap ? qt : sh.qcap;
+                if (rh < rt) {
+                    if (idle) { atomicSub(&sh.idle, 1); idle = false; }
+                    if (atomicCAS(&sh.rqhead, rh, rh + 1) == rh) { act = 2; h = read_entry(sd.scr.rq, rh, sh); }
+                } else if (head < tail) {
+                    if (idle) { atomicSub(&sh.idle, 1); idle = false; }
+                    const int want = tail - head < 32 ? tail - head : 32;
+                    if (atomicCAS(&sh.qhead, head, head + want) == head) { act = 1; h = head; m = want; }
+                } else {
+                    if (!idle) { __threadfence_block(); atomicAdd(&sh.idle, 1); idle = true; }
+                    /* all idle with nothing queued and nodes left: nothing can release them */
+                    if (quiescent(sh) && vload(sh.ndone) < total) {
+                        atomicCAS(&sh.status, 0, 3);
+                        act = 3;
+                    }
+                }
+                if (act == 1 || act == 2) {
+                    since = clock64();
+                } else if (act == 0 && clock64() - since > FD_WAIT_CYCLES) {
+                    atomicCAS(&sh.status, 0, 8);   /* no work for this worker for too long */
+                    act = 3;
+                }
+            }
+        }
+        act = __shfl_sync(0xffffffffu, act, 0);
+        if (act == 3) break;
+        h = __shfl_sync(0xffffffffu, h, 0);
+        if (act == 1) {
+            m = __shfl_sync(0xffffffffu, m, 0);
+            int e = -1;
+            if (lane < m) {
+                const volatile int *q = queue + h + lane;
+                e = *q;
+                for (int spin = 0; e < 0 && spin < FD_QSPIN; spin++) {
+                    __nanosleep(32);
+                    e = *q;
+                }
+                if (e < 0) atomicCAS(&sh.status, 0, 9);   /* a claimed entry never written */
+            }
+            __threadfence_block();
+            warp_chunk(sd, sh, cs, ws, e, false, 0.f, 0.f, dag, cn);
+            chunks++;
+            continue;
+        }
+        if (act == 2) {
+            __threadfence_block();
+            if (h >= 0) resume_waiter(sd, sh, cs, ws, h, dag, cn);
+            continue;
+        }
+        __nanosleep(64);
+    }
+    if (lane == 0 && chunks) atomicAdd(reinterpret_cast<unsigned long long *>(&sh.rounds), (unsigned long long)chunks);
+}
+
 /* Walk the current face (parameters in sh) in dependency order. */
-__device__ void face_walk(const fd_station_dev &sd, Shared &sh, Smem &sm, bool dag_in_smem, Counters &cn)
+__device__ void face_walk(const fd_station_dev &sd, Shared &sh, CtaSmem &cs, WarpSmem &ws, unsigned char *dag,
+                          Counters &cn)
 {
     const int n = sh.n, nuf = sh.nuf, nvf = n / nuf;
     const int tid = threadIdx.x;
     const float *T = sd.T;
     const fdn_frame fr = frame_of(sh.face);
-    unsigned char *dag = dag_indeg(sd, sm, dag_in_smem);
     unsigned char *emask = dag + sh.n_pad;
+    int *queue = sd.scr.queue;
     FD_TIC(t0);
     /* trial descriptors of this face */
-    for (int k = tid; k < FDN_NTRIAL; k += blockDim.x) sm.desc[k] = c_desc[sh.face * FDN_NTRIAL + k];
+    for (int k = tid; k < FDN_NTRIAL; k += blockDim.x) cs.desc[k] = c_desc[sh.face * FDN_NTRIAL + k];
     /* keys: time of the inner-layer neighbour, then fill index */
     for (int i = tid; i < n; i += blockDim.x) {
         int xyz[3];
@@ -766,8 +985,17 @@ __device__ void face_walk(const fd_station_dev &sd, Shared &sh, Smem &sm, bool d
         xyz[fr.axis_n] = sh.layer + fr.inner;
         const float tin = T[((long long)xyz[2] * sd.g.ny + xyz[1]) * sd.g.nx + xyz[0]];
         sd.scr.key[i] = ((unsigned long long)okey32(tin) << 32) | (unsigned)i;
+        sd.scr.pst[i] = -1;
+        queue[i] = -1;
+        sd.scr.rq[2 * i] = -1;
+        sd.scr.rq[2 * i + 1] = -1;
     }
-    if (tid == 0) { sh.cnt[0] = 0; sh.cnt[1] = 0; sh.ndef = 0; sh.exitkey = 0ull; }
+    if (tid == 0) {
+        sh.qhead = sh.qtail = sh.rqhead = sh.rqtail = sh.idle = sh.ndone = 0;
+        sh.qcap = n;
+        sh.rqcap = 2 * n;
+        sh.exitkey = 0ull;
+    }
     __syncthreads();
     /* earlier-neighbour masks and in-degrees */
     for (int i = tid; i < n; i += blockDim.x) {
@@ -784,67 +1012,14 @@ __device__ void face_walk(const fd_station_dev &sd, Shared &sh, Smem &sm, bool d
         }
         emask[i] = (unsigned char)em;
         dag[i] = (unsigned char)__popc(em);
-        if (em == 0) sd.scr.wl[0][atomicAdd(&sh.cnt[0], 1)] = i;
+        if (em == 0) enqueue(queue, sh, i);
     }
     __syncthreads();
     FD_TOC(0, t0);
-    int cur = 0;
-    long long rounds = 0;
-    const long long max_rounds = 2ll * n + 8;
-    for (;;) {
-        FD_TIC(tr);
-        __syncthreads();
-        const int ncur = sh.cnt[cur];
-        const int ndef = sh.ndef;
-        if (++rounds > max_rounds) {
-            if (tid == 0) sh.status = 3;
-            break;
-        }
-        if (ncur == 0) {
-            if (ndef == 0) break;
-            /* the deferred point with the smallest key: every point below it is done */
-            unsigned long long lm = ~0ull;
-            for (int j = tid; j < ndef; j += blockDim.x) {
-                const unsigned long long k = sd.scr.key[sd.scr.deferred[j]];
-                lm = k < lm ? k : lm;
-            }
-            const unsigned long long dmin = block_min_u64(lm, sh);
-            /* the last writer before it in sort order */
-            unsigned long long lw = 0ull;
-            for (int i = tid; i < n; i += blockDim.x) {
-                const unsigned long long k = sd.scr.key[i];
-                if (k < dmin && dag[i] == 0xFFu && !isnan(sd.scr.rec[i].x)) lw = k > lw ? k : lw;
-            }
-            const unsigned long long wkey = block_max_u64(lw, sh);
-            const int d = (int)(dmin & 0xffffffffu);
-            float t0 = sh.carry_t0, t4 = sh.carry_t4;
-            if (wkey) {
-                const float2 r = sd.scr.rec[(int)(wkey & 0xffffffffu)];
-                t0 = r.x;
-                t4 = r.y;
-            }
-            if (tid == 0) {
-                for (int j = 0; j < ndef; j++)
-                    if (sd.scr.deferred[j] == d) { sd.scr.deferred[j] = sd.scr.deferred[ndef - 1]; break; }
-                sh.ndef = ndef - 1;
-                sh.deferred++;
-            }
-            __syncthreads();
-            const int one[1] = {d};
-            run_chunk(sd, sh, sm, one, 1, true, t0, t4, cur, dag, cn);
-            FD_TOC(5, tr);
-            continue;
-        }
-        if (tid == 0) { sh.cnt[cur ^ 1] = 0; sh.rounds++; }
-        __syncthreads();
-        FD_TOC(4, tr);
-        for (int c0 = 0; c0 < ncur; c0 += FD_CHUNK) {
-            const int m = ncur - c0 < FD_CHUNK ? ncur - c0 : FD_CHUNK;
-            run_chunk(sd, sh, sm, sd.scr.wl[cur] + c0, m, false, 0.f, 0.f, cur ^ 1, dag, cn);
-        }
-        cur ^= 1;
-    }
+    FD_TIC(tw);
+    run_walk(sd, sh, cs, ws, queue, n, dag, cn);
     __syncthreads();
+    FD_TOC(4, tw);
     if (tid == 0) {
         if (sh.exitkey) {
             const float2 r = sd.scr.rec[(int)(sh.exitkey & 0xffffffffu)];
@@ -890,7 +1065,7 @@ __device__ void setup_face(const fd_station_dev &sd, Shared &sh, int face)
 
 /* One sweep of face F as a plane-pipelined dependency graph.  Leaves walls, flags and radius as
  * the radius loop of src/sphfd.c:1018-5566 would. */
-__device__ void pipelined_sweep(const fd_station_dev &sd, Shared &sh, Smem &sm, Counters &cn, int F)
+__device__ void pipelined_sweep(const fd_station_dev &sd, Shared &sh, CtaSmem &cs, WarpSmem &ws, Counters &cn, int F)
 {
     const int tid = threadIdx.x;
     const fdn_frame fr = frame_of(F);
@@ -916,15 +1091,19 @@ __device__ void pipelined_sweep(const fd_station_dev &sd, Shared &sh, Smem &sm, 
         sh.dflag[F] = flag;
         sh.radius = radius;
         sh.rad0 = rad0;
-        sh.qtail = 0;
+        sh.qhead = sh.qtail = sh.rqhead = sh.rqtail = sh.idle = sh.ndone = 0;
+        sh.qcap = (int)((long long)np * sh.n);
+        sh.rqcap = 0;
         sh.exitkey = 0ull;
         sh.pipelined = 1;
     }
-    for (int k = tid; k < FDN_NTRIAL; k += blockDim.x) sm.desc[k] = c_desc[F * FDN_NTRIAL + k];
+    for (int k = tid; k < FDN_NTRIAL; k += blockDim.x) cs.desc[k] = c_desc[F * FDN_NTRIAL + k];
     __syncthreads();
     const int np = sh.np, nplane = sh.n, nuf = sh.nuf, nvf = nplane > 0 ? nplane / nuf : 0;
     const long long total = (long long)np * nplane;
     if (total > 0) {
+        for (long long id = tid; id < total; id += blockDim.x) sd.scr.pqueue[id] = -1;
+        __syncthreads();
         /* counters: plane 0 reads the static wall layer, so its in-plane order is known now */
         const int wall_layer = sh.player0 + fr.inner;
         for (long long id = tid; id < total; id += blockDim.x) {
@@ -938,24 +1117,11 @@ __device__ void pipelined_sweep(const fd_station_dev &sd, Shared &sh, Smem &sm, 
                 wd -= (unsigned)__popc(inr & ~em) << 8;
             }
             sd.scr.pcount[id] = wd;
-            if (wd == 0u) sd.scr.pqueue[atomicAdd(&sh.qtail, 1)] = (int)id;
-        }
-        long long head = 0, steps = 0;
-        for (;;) {
-            __syncthreads();
-            const long long tail = sh.qtail;
-            if (head >= total || sh.status) break;
-            const long long avail = tail - head;
-            if (avail <= 0 || ++steps > total + 8) {
-                if (tid == 0) sh.status = 5;   /* cannot happen: every node is queued exactly once */
-                break;
-            }
-            const int m = avail < FD_CHUNK ? (int)avail : FD_CHUNK;
-            run_chunk(sd, sh, sm, sd.scr.pqueue + head, m, false, 0.f, 0.f, 0, sd.scr.dag, cn);
-            head += m;
+            if (wd == 0u) enqueue(sd.scr.pqueue, sh, (int)id);
         }
         __syncthreads();
-        if (tid == 0) sh.rounds += steps;
+        run_walk(sd, sh, cs, ws, sd.scr.pqueue, (int)total, nullptr, cn);
+        __syncthreads();
     }
     if (tid == 0) {
         if (sh.exitkey) {
@@ -971,7 +1137,6 @@ __device__ void pipelined_sweep(const fd_station_dev &sd, Shared &sh, Smem &sm, 
     __syncthreads();
 }
 
-/* ---------------------------------------------------------------------------------------------- */
 /* source box (src/sphfd.c:724-825)                                                                */
 
 __device__ void init_field(const fd_station_dev &sd)
@@ -1014,14 +1179,15 @@ __global__ void __launch_bounds__(FD_BLOCK, 1) fd_solve(const fd_station_dev *st
 {
     __shared__ Shared sh;
     extern __shared__ __align__(16) unsigned char fd_dyn_smem[];
-    Smem &sm = *reinterpret_cast<Smem *>(fd_dyn_smem);
+    CtaSmem &cs = *reinterpret_cast<CtaSmem *>(fd_dyn_smem);
+    WarpSmem &ws = reinterpret_cast<WarpSmem *>(fd_dyn_smem + kCtaSmemBytes)[threadIdx.x >> 5];
     if ((int)blockIdx.x >= nst) return;
     const fd_station_dev &sd = stations[blockIdx.x];
     const int tid = threadIdx.x;
     unsigned long long t_start = 0;
     if (tid == 0) asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t_start));
     /* the dependency bytes of the station's largest face go to shared memory when they fit */
-    const bool dag_in_smem = 2ll * sd.max_face_pad <= dag_smem_bytes;
+    unsigned char *dag = 2ll * sd.max_face_pad <= dag_smem_bytes ? fd_dyn_smem + kSmemBase : sd.scr.dag;
     if (sd.init_mode == 0) init_field(sd);
     if (tid == 0) {
         for (int f = 0; f < 6; f++) { sh.wall[f] = sd.wall[f]; sh.dflag[f] = sd.dflag[f]; }
@@ -1068,7 +1234,7 @@ __global__ void __launch_bounds__(FD_BLOCK, 1) fd_solve(const fd_station_dev *st
             }
             piped = !__syncthreads_or(bad);
         }
-        if (piped) pipelined_sweep(sd, sh, sm, cn, act);
+        if (piped) pipelined_sweep(sd, sh, cs, ws, cn, act);
         while (!piped && sh.rad0
                && (sh.dflag[0] || sh.dflag[1] || sh.dflag[2] || sh.dflag[3] || sh.dflag[4] || sh.dflag[5])
                && sh.status == 0) {
@@ -1077,7 +1243,7 @@ __global__ void __launch_bounds__(FD_BLOCK, 1) fd_solve(const fd_station_dev *st
                     if (!sh.dflag[face]) continue;
                     if (tid == 0) setup_face(sd, sh, face);
                     __syncthreads();
-                    if (sh.n > 0) face_walk(sd, sh, sm, dag_in_smem, cn);
+                    if (sh.n > 0) face_walk(sd, sh, cs, ws, dag, cn);
                     __syncthreads();
                     if (tid == 0) {
                         /* move the wall outward (e.g. src/sphfd.c:1762-1764) */
@@ -1142,6 +1308,7 @@ __global__ void __launch_bounds__(FD_BLOCK, 1) fd_solve(const fd_station_dev *st
         asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t_end));
         o->t_start_ns = (int64_t)t_start;
         o->t_end_ns = (int64_t)t_end;
+        o->pipelined_sweeps = (int32_t)sh.psweeps;
     }
 }
 
@@ -1164,7 +1331,7 @@ extern "C" cudaError_t fdk_launch_solve(const fd_station_dev *stations, int nst,
     int dev = 0, optin = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    const long long base = (long long)sizeof(fdk::Smem);
+    const long long base = (long long)fdk::kSmemBase;
     const long long want = base + 2 * max_face_pad;
     const long long bytes = want <= optin - 1024 ? want : base;
     const cudaError_t e = cudaFuncSetAttribute(fdk::fd_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);

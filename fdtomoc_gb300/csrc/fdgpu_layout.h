@@ -64,22 +64,25 @@ typedef struct {
     int32_t sweeps;
     int64_t node_updates;
     int64_t faces;
-    int64_t rounds;          /* dependency rounds over all faces */
+    int64_t rounds;          /* warp chunks over all walks */
     int64_t deferred;        /* points that waited for an earlier point's (t0,t4) */
     int64_t stencils[5];     /* stencil evaluations by kind (3d ne 2d nf 1d), after pruning */
     int32_t restart_wall[8]; /* how often each wall (1..6) was chosen for a restart */
-    int64_t phase_cycles[6]; /* with FDGPU_PHASE_TIMERS: SM cycles in face set-up, phases A, B, C,
-                                round bookkeeping, deferred resolution (zero otherwise) */
+    int64_t phase_cycles[6]; /* with FDGPU_PHASE_TIMERS: warp cycles summed over warps in face
+                                set-up, phases A, B, C and the face walks (zero otherwise) */
     int64_t t_start_ns, t_end_ns; /* GPU global timer when the station's solve began and ended */
+    int32_t pipelined_sweeps;
+    int32_t pad;
 } fd_station_stats;
 
-/* Face-walk scratch of one station, sized for its largest face. */
+/* Face-walk scratch of one station, sized for its largest face m (34 bytes per point):
+ * key 8m | rec 8m | pst 4m | queue 4m | rq 8m | dag 2m (+32). */
 typedef struct {
     unsigned long long *key;   /* (time bits of the inner-layer node << 32) | fill index */
-    int *indeg;                /* earlier neighbours still pending; -1 once the point is done */
-    int *wl[2];                /* ready lists */
     float2 *rec;               /* (t0,t4) the point left in the stencil state; NaN if no writer */
-    int *deferred;             /* points waiting for an earlier point's (t0,t4) */
+    int *pst;                  /* -1 pending, -2 done, >= 0 pending with that point waiting on it */
+    int *queue;                /* ready points, one entry per point */
+    int *rq;                   /* points waiting for an earlier point's (t0,t4), 2 entries per point */
     unsigned char *dag;        /* in-degree and earlier-neighbour bytes (2 per point) when they do
                                   not fit in shared memory */
     /* plane-pipelined sweeps (NULL: not available, every face is walked on its own):

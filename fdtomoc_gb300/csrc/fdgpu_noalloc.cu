@@ -195,10 +195,9 @@ extern "C" int fdgpu_solve_noalloc(const fdgpu_station *st, const float *d_slown
     unsigned char *fb = base + p.face;
     d.scr.key = reinterpret_cast<unsigned long long *>(fb);
     d.scr.rec = reinterpret_cast<float2 *>(fb + 8 * m);
-    d.scr.indeg = reinterpret_cast<int *>(fb + 16 * m);
-    d.scr.wl[0] = reinterpret_cast<int *>(fb + 20 * m);
-    d.scr.wl[1] = reinterpret_cast<int *>(fb + 24 * m);
-    d.scr.deferred = reinterpret_cast<int *>(fb + 28 * m);
+    d.scr.pst = reinterpret_cast<int *>(fb + 16 * m);
+    d.scr.queue = reinterpret_cast<int *>(fb + 20 * m);
+    d.scr.rq = reinterpret_cast<int *>(fb + 24 * m);
     d.scr.dag = fb + 32 * m;
     d.max_face_pad = p.max_face_pad;
     d.stats = reinterpret_cast<fd_station_stats *>(base + p.stats);
@@ -226,6 +225,8 @@ extern "C" int fdgpu_solve_noalloc(const fdgpu_station *st, const float *d_slown
         for (int j = 0; j < 8; j++) stats->restart_wall[j] = hs.restart_wall[j];
         stats->t_start_ns = hs.t_start_ns;
         stats->t_end_ns = hs.t_end_ns;
+        stats->pipelined_sweeps = hs.pipelined_sweeps;
+        stats->detail = hs.status;
     }
     return hs.status ? FDGPU_ESCHED : FDGPU_OK;
 }

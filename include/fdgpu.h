@@ -36,7 +36,7 @@ enum {
     FDGPU_EIO = -4,      /* a file could not be read or written */
     FDGPU_EPAR = -5,     /* a required par parameter is missing or a value is invalid */
     FDGPU_ESOURCE = -6,  /* the source is outside the grid (src/sphfd.c:533-538) */
-    FDGPU_ESCHED = -7,   /* internal: a face walk exceeded its round bound */
+    FDGPU_ESCHED = -7,   /* internal: a walk's schedule check failed (fdgpu_stats.detail says which) */
     FDGPU_ENODEV = -8,   /* no CUDA device */
     FDGPU_ETOOBIG = -9   /* the problem needs more than fdgpu_solve_noalloc's static scratch */
 };
@@ -69,13 +69,18 @@ typedef struct {
     int32_t sweeps;          /* sweeps run (1 + restarts) */
     int64_t node_updates;    /* face-point evaluations */
     int64_t faces;
-    int64_t rounds;          /* dependency rounds of the face walks */
+    int64_t rounds;          /* chunks of up to 32 ready nodes evaluated by one warp */
     int64_t deferred;        /* points that took the stale (t0,t4) of an earlier point */
     int64_t stencils[5];     /* stencil evaluations: 3-D, new-edge, 2-D, new-face, 1-D */
     int32_t restart_wall[8]; /* restarts per wall 1..6 */
-    int64_t phase_cycles[6]; /* profiling builds only: cycles in face set-up, the three evaluation
-                                phases, round bookkeeping and deferred resolution */
+    int64_t phase_cycles[6]; /* profiling builds only: warp cycles summed over the warps in face
+                                set-up, the three evaluation phases and the face walks */
     int64_t t_start_ns, t_end_ns; /* GPU global timer (ns) at the start and end of this solve */
+    int32_t pipelined_sweeps; /* sweeps walked as one plane-pipelined dependency graph */
+    int32_t detail;           /* on FDGPU_ESCHED, the check that failed: 3 nodes left that nothing
+                                 releases, 4 sweep bound, 6 a pipelined sweep met a point needing an
+                                 earlier point's stencil state, 8 a worker waited too long, 9 a
+                                 claimed queue entry was never written, 10 a node queued twice */
 } fdgpu_stats;
 
 int fdgpu_create(int device, fdgpu_ctx **out);
