@@ -34,6 +34,7 @@ METRIC = "station fields/s (batched, 201x201x81, bit-identical to reference)"
 UNIT = "station fields/s"
 STATIONS_PER_GPU = 64
 CONFIG_NAME = "64 stations, 201x201x81 grid, 0.005deg x 0.005deg x 0.5km (config 2)"
+CONFIG1_NAME = "1 station, 61x61x31 grid, 0.01deg x 0.01deg x 1km (config 1, profiling case)"
 ALGO_BYTES_PER_NODE_UPDATE = 12  # slowness read, time read, time write
 
 
@@ -43,9 +44,14 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--stations", type=int, default=STATIONS_PER_GPU)
+    ap.add_argument("--stations", type=int, default=None, help="stations per GPU (default 64; config 1: 1)")
+    ap.add_argument("--config", type=int, default=2, choices=[1, 2],
+                    help="2: the benchmark workload; 1: the one-station 61x61x31 case, for profiling")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    return ap.parse_args()
+    args = ap.parse_args()
+    if args.stations is None:
+        args.stations = STATIONS_PER_GPU if args.config == 2 else 1
+    return args
 
 
 def dist_env():
@@ -53,11 +59,11 @@ def dist_env():
             int(os.environ.get("LOCAL_RANK", 0)))
 
 
-def workload(rank: int, n: int):
-    """The config-2 model and this rank's n stations (weak scaling: rank r takes its own stations)."""
+def workload(rank: int, n: int, cfg: int = 2):
+    """The model of config cfg and this rank's n stations (weak scaling: rank r takes its own)."""
     from fdtomoc_gb300 import workloads as W
-    g, v, _ = W.config(2)
-    sts = W.stations(g, n * (rank + 1), 2)[n * rank:]
+    g, v, _ = W.config(cfg)
+    sts = W.stations(g, n * (rank + 1), cfg)[n * rank:]
     return g, v, sts
 
 
@@ -175,7 +181,7 @@ def run_gpu(args):
     rank, world, local = dist_env()
     n = args.stations
     case_dir = tempfile.mkdtemp(prefix=f"fdbench_r{rank}_")
-    g, v, sts = workload(rank, n)
+    g, v, sts = workload(rank, n, args.config)
     write_case(case_dir, g, v, sts)
     names = [s["name"] for s in sts]
 
@@ -318,9 +324,10 @@ def run_gpu(args):
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64 stencils / f32 fields", "data": "synthetic (seeded, config 2 recipe)",
-            "config": {"workload": CONFIG_NAME, "stations_per_gpu": n, "grid": [g.nx, g.ny, g.nz],
-                       "l2": "inputs larger than L2 (64 fields x 13 MB + 13 MB model)", "parallelism": f"stations x{world}"},
+            "vs_baseline": None, "dtype": "f64 stencils / f32 fields", "data": f"synthetic (seeded, config {args.config} recipe)",
+            "config": {"workload": CONFIG_NAME if args.config == 2 else CONFIG1_NAME, "stations_per_gpu": n, "grid": [g.nx, g.ny, g.nz],
+                       "l2": ("inputs larger than L2 (64 fields x 13 MB + 13 MB model)" if args.config == 2
+                              else "small case: inputs fit in L2"), "parallelism": f"stations x{world}"},
             "node_updates_per_s": nu_step * world / (ms_step / 1e3),
             "latency_ms": {"p50": p50, "p99": p99, "what": "station completion time within a batch"},
             "plain": {"ms_per_station": plain_ms, "fields_per_s": 1e3 / plain_ms,
@@ -354,7 +361,7 @@ def run_reference(args):
     n = args.stations
     ncores = os.cpu_count() or 1
     case_dir = tempfile.mkdtemp(prefix="fdbench_ref_")
-    g, v, sts = workload(0, n)
+    g, v, sts = workload(0, n, args.config)
     write_case(case_dir, g, v, sts)
     names = [s["name"] for s in sts]
     sample = names[:min(ncores, n)]
@@ -370,8 +377,8 @@ def run_reference(args):
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64 stencils / f32 fields", "data": "synthetic (seeded, config 2 recipe)",
-        "config": {"workload": CONFIG_NAME, "stations_per_gpu": n, "grid": [g.nx, g.ny, g.nz],
+        "vs_baseline": None, "dtype": "f64 stencils / f32 fields", "data": f"synthetic (seeded, config {args.config} recipe)",
+        "config": {"workload": CONFIG_NAME if args.config == 2 else CONFIG1_NAME, "stations_per_gpu": n, "grid": [g.nx, g.ny, g.nz],
                    "parallelism": f"{len(sample)} processes x 1 thread"},
         "node_updates_per_s": sum(nus) / tot,
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": len(sample), "kind": "port",

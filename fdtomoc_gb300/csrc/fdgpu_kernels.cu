@@ -30,6 +30,7 @@
 
 #include "fdgpu_eval.cuh"
 #include "fdgpu_trials.cuh"
+#include "fdgpu_bound.cuh"
 #include "fdgpu_layout.h"
 
 #define FD_WARPS 12                 /* independent workers per station */
@@ -230,6 +231,9 @@ struct Counters {
 
 #define NB_PAD 19                    /* context row stride: the 32 rows fall on distinct banks */
 #define FD_WAIT_CYCLES (4ll << 30)   /* about 2 s at the maximum SM clock */
+#ifndef FD_FACE_WARPS
+#define FD_FACE_WARPS FD_WARPS       /* workers that take part in a face walk */
+#endif
 #define FD_QSPIN (1 << 22)           /* polls of an unwritten queue entry before giving up */
 
 #define FD_DESC_ROW(F)                                                                              \
@@ -481,6 +485,7 @@ __device__ unsigned stale_pair(const CtaSmem &cs, WarpSmem &ws, int slot, unsign
     }
     ws.s0[slot] = s0;
     ws.s4[slot] = s4;
+    ws.res[slot][TK_NF] = g1;   /* for filter_2d: the new-face value is never precomputed */
     unsigned add = 0;
     for (int K = TK_2D0; K < TK_NF; K++) {
         if (!((gm >> K) & 1u)) continue;
@@ -489,6 +494,37 @@ __device__ unsigned stale_pair(const CtaSmem &cs, WarpSmem &ws, int slot, unsign
         if (!prunable(fl, g1)) add |= 1u << K;
     }
     return add;
+}
+
+/* Drop the queued 2-D items whose single-precision lower bound shows they cannot lower the
+ * running minimum entering the 2-D block (kept in res[slot][TK_NF]); their value is recorded as the
+ * rejection value, which leaves the minimum and the head-wave test as the true value would.
+ * Compacts items[0..n) in place and returns the number left. */
+__device__ int filter_2d(const fd_station_dev &sd, const CtaSmem &cs, WarpSmem &ws, int n, int lane)
+{
+    int out = 0;
+    for (int j0 = 0; j0 < n; j0 += 32) {
+        const int j = j0 + lane;
+        unsigned it = 0;
+        bool keep = false;
+        if (j < n) {
+            it = ws.items[j];
+            const int slot = (int)(it >> 5), K = (int)(it & 31);
+            const TrialDesc &d = cs.desc[K];
+            const float *t18 = ws.t[slot];
+            const float fl = fmaxf(fmaxf(fmaxf(t18[d.slot[1]], t18[d.slot[2]]), fmaxf(t18[d.slot[3]], ws.s0[slot])),
+                                   ws.s4[slot]);
+            const float lo = lower_2d(d, t18, ws.s[slot], sd.g, ws.z[slot], ws.y[slot], fl);
+            if (bound_prunes(lo, ws.res[slot][TK_NF]))
+                ws.res[slot][K] = 1.e11;
+            else
+                keep = true;
+        }
+        const unsigned b = __ballot_sync(0xffffffffu, keep);
+        if (keep) ws.items[out + __popc(b & ((1u << lane) - 1u))] = (unsigned short)it;
+        out += __popc(b);
+    }
+    return out;
 }
 
 /* ---------------------------------------------------------------------------------------------- */
@@ -764,7 +800,9 @@ __device__ void warp_chunk(const fd_station_dev &sd, Shared &sh, const CtaSmem &
     const float p0 = permissive ? lo : it0, p4 = permissive ? lo : it4;
     if (valid) em |= stale_pair(cs, ws, lane, gm, em, p0, p4);
     __syncwarp();
-    const int n2 = push_items(ws.items, 0, em, TK_2D0, TK_NF, lane);
+    int n2 = push_items(ws.items, 0, em, TK_2D0, TK_NF, lane);
+    __syncwarp();
+    n2 = filter_2d(sd, cs, ws, n2, lane);
     __syncwarp();
     eval_items(sd, cs, ws, n2, lane, cn);
     __syncwarp();
@@ -914,7 +952,7 @@ __device__ void run_walk(const fd_station_dev &sd, Shared &sh, const CtaSmem &cs
                 if (rh < rt) {
                     if (idle) { atomicSub(&sh.idle, 1); idle = false; }
                     if (atomicCAS(&sh.rqhead, rh, rh + 1) == rh) { act = 2; h = read_entry(sd.scr.rq, rh, sh); }
-                } else if (head < tail) {
+                } else if (head < tail && (sh.pipelined || (int)(threadIdx.x >> 5) < FD_FACE_WARPS)) {
                     if (idle) { atomicSub(&sh.idle, 1); idle = false; }
                     const int want = tail - head < 32 ? tail - head : 32;
                     if (atomicCAS(&sh.qhead, head, head + want) == head) { act = 1; h = head; m = want; }
@@ -1215,6 +1253,7 @@ __global__ void __launch_bounds__(FD_BLOCK, 1) fd_solve(const fd_station_dev *st
     while (sh.reverse > -1 && sh.status == 0) {
         if (tid == 0) for (int k = 0; k < 8; k++) sh.headw[k] = 0;
         __syncthreads();
+        FD_TIC(tsweep);
         /* A sweep with one active face (every sweep after a restart) walks full planes.  It runs as
          * one plane-pipelined graph when no point can need an earlier point's stencil state: every
          * time below 1e9 makes every corner guard that is inside the grid pass (so each point calls
@@ -1263,6 +1302,7 @@ __global__ void __launch_bounds__(FD_BLOCK, 1) fd_solve(const fd_station_dev *st
             __syncthreads();
         }
         if (tid == 0) {
+            if (sh.sweeps == 0) FD_TOC(5, tsweep);   /* profiling builds: the first sweep's cycles */
             sh.sweeps++;
             /* restart test (src/sphfd.c:5570-5676) */
             const int *hw = sh.headw;
