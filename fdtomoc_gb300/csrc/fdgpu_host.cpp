@@ -190,6 +190,19 @@ long long max_face(const fdgpu_station &s)
 }
 
 constexpr size_t kScratchPerPoint = 8 + 4 + 4 + 4 + 8 + 4 + 2;
+/* sweep-graph arrays per grid node: stencil-state record, counter, queue, earlier-neighbour byte;
+ * then the face instances, wait pairs, parked points and resume queue */
+constexpr size_t kGraphPerNode = 8 + 4 + 4 + 1;
+
+size_t graph_node_bytes(size_t nn) { return (nn * kGraphPerNode + 255) & ~(size_t)255; }
+
+size_t graph_bytes(const fdgpu_station &s)
+{
+    const size_t nn = (size_t)s.nx * s.ny * s.nz;
+    const size_t ninst = (size_t)s.nx + s.ny + s.nz + 8;
+    return graph_node_bytes(nn) + ((ninst * sizeof(fd_ginst) + 255) & ~(size_t)255)
+           + 8 * (size_t)FD_GWAIT_CAP + 8 * (size_t)FD_GPARK_CAP + 4 * (size_t)FD_GRQ_CAP;
+}
 
 int check_station(const fdgpu_station &s)
 {
@@ -248,7 +261,7 @@ extern "C" const char *fdgpu_strerror(int s)
     case FDGPU_EIO: return "file I/O error";
     case FDGPU_EPAR: return "missing or invalid par parameter";
     case FDGPU_ESOURCE: return "source outside the grid";
-    case FDGPU_ESCHED: return "face walk exceeded its bound";
+    case FDGPU_ESCHED: return "a schedule check of the solve failed (fdgpu_stats.detail says which)";
     case FDGPU_ENODEV: return "no CUDA device";
     case FDGPU_ETOOBIG: return "problem exceeds the static scratch of the no-allocation entry point";
     default: return "unknown status";
@@ -297,11 +310,11 @@ extern "C" int fdgpu_solve_device(fdgpu_ctx *ctx, int n, const fdgpu_station *st
     }
     /* scratch and per-station records */
     std::vector<size_t> off(n + 1, 0);
-    /* per station: face scratch, then the plane-pipelining arrays (9 bytes per grid node) */
+    /* per station: face scratch, then the sweep-graph arrays */
     auto nodes = [&](int k) { return (size_t)st[k].nx * st[k].ny * st[k].nz; };
     for (int k = 0; k < n; k++)
         off[k + 1] = off[k] + ((((size_t)max_face(st[k]) + 16) * kScratchPerPoint + 255) & ~(size_t)255)
-                     + ((nodes(k) * 9 + 255 + 512) & ~(size_t)255);
+                     + graph_bytes(st[k]);
     FD_CU(ctx, ctx->scratch.ensure(off[n]));
     FD_CU(ctx, ctx->stations.ensure(sizeof(fd_station_dev) * n));
     FD_CU(ctx, ctx->stats.ensure(sizeof(fd_station_stats) * n));
@@ -360,11 +373,22 @@ extern "C" int fdgpu_solve_device(fdgpu_ctx *ctx, int n, const fdgpu_station *st
         d.scr.rq = reinterpret_cast<int *>(base + 24 * m);
         d.scr.dag = reinterpret_cast<unsigned char *>(base + 32 * m);
         {
+            /* 8-byte records first, then the 4-byte arrays, then the bytes */
             char *pb = base + ((((size_t)m + 16) * kScratchPerPoint + 255) & ~(size_t)255);
             const size_t nn = nodes(k);
-            d.scr.pcount = reinterpret_cast<unsigned *>(pb);
-            d.scr.pqueue = reinterpret_cast<int *>(pb + 4 * nn);
-            d.scr.pemask = reinterpret_cast<unsigned char *>(pb + 8 * nn);
+            d.scr.grec = reinterpret_cast<float2 *>(pb);
+            d.scr.gcnt = reinterpret_cast<unsigned *>(pb + 8 * nn);
+            d.scr.gqueue = reinterpret_cast<int *>(pb + 12 * nn);
+            d.scr.gemask = reinterpret_cast<unsigned char *>(pb + 16 * nn);
+            char *tb = pb + graph_node_bytes(nn);
+            d.scr.ginst_cap = s.nx + s.ny + s.nz + 8;
+            d.scr.ginst = reinterpret_cast<fd_ginst *>(tb);
+            tb += ((size_t)d.scr.ginst_cap * sizeof(fd_ginst) + 255) & ~(size_t)255;
+            d.scr.gwait = reinterpret_cast<int2 *>(tb);
+            tb += 8 * (size_t)FD_GWAIT_CAP;
+            d.scr.gpark = reinterpret_cast<int2 *>(tb);
+            tb += 8 * (size_t)FD_GPARK_CAP;
+            d.scr.grq = reinterpret_cast<int *>(tb);
         }
         d.max_face_pad = ((long long)m + 15) & ~15LL;
         max_pad = std::max(max_pad, d.max_face_pad);

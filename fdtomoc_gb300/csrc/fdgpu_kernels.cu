@@ -126,15 +126,25 @@ struct Shared {
     int radius, rad0, reverse, headpref;
     int headw[8];
     float carry_t0, carry_t4;
-    /* current walk: ready queue, queue of points waiting for an inherited stencil state, idle
-     * workers, finished nodes */
-    int qhead, qtail, qcap, rqhead, rqtail, rqcap, idle, ndone;
+    /* current walk: ready queues (one per face in a sweep graph; a face walk uses queue 0), the
+     * queue of points resuming a search for an inherited stencil state, idle workers, finished
+     * nodes, parked points */
+    int nq;
+    int qhead[6], qtail[6], qcap[6], qbase[6];
+    int rqhead, rqtail, rqcap, idle, ndone, npark;
     unsigned long long exitkey;
-    /* current face */
+    /* current face of a face walk */
     int face, layer, ulo, uhi, vlo, vhi, nuf, n, n_pad;
     long long su, sv, sn, ssu, ssv, ssn;
     int nu, nv;
     int status;
+    /* current sweep graph: on/off, face instances, points; per face, the 27-bit masks of the
+     * neighbour offsets a node of that face reads, and of those in its inner plane */
+    int graph, gok, ninst, single, nodefer, nwait;
+    unsigned gfaces;
+    long long gM;
+    unsigned ctxm[6], innm[6];
+    void *gsm;
     unsigned long long red[FD_BLOCK / 32];
     unsigned long long bcast;
     /* statistics */
@@ -143,9 +153,7 @@ struct Shared {
     int sweeps;
     int restart_wall[8];
     long long cyc[6];
-    /* plane-pipelined sweep: on/off, number of planes, layer of plane 0 */
-    int pipelined, np, player0;
-    long long psweeps;
+    long long gsweeps;
 };
 
 /* face frame for a face number known only at run time */
@@ -210,31 +218,25 @@ struct Counters {
 /* ---------------------------------------------------------------------------------------------- */
 /* warp workers                                                                                    */
 /*                                                                                                 */
-/* A walk — one face, or one plane-pipelined sweep — is a dependency graph whose ready nodes sit   */
-/* in a queue.  Every warp of the CTA is an independent worker: it claims up to 32 ready nodes,     */
-/* evaluates them (one lane per node for the per-node steps, the stencil trials of all its nodes   */
-/* spread over the 32 lanes), commits them and queues the nodes they complete.  Warps meet only at */
-/* shared-memory counters, so the FP64 work of some warps hides the memory and control latency of  */
-/* the others, and a node starts as soon as its own inputs are final instead of at the next round. */
+/* A walk — one face, or a whole sweep as one graph — is a dependency graph whose ready nodes sit   */
+/* in queues.  Every warp of the CTA is an independent worker: it claims up to 32 ready nodes of    */
+/* one face direction, evaluates them (one lane per node for the per-node steps, the stencil       */
+/* trials of all its nodes spread over the 32 lanes), commits them and queues the nodes they       */
+/* complete.  Warps meet only at shared-memory counters, so the FP64 work of some warps hides the  */
+/* memory and control latency of the others, and a node starts as soon as its own inputs are      */
+/* final.                                                                                          */
 /*                                                                                                 */
-/* Queue: positions are taken with an atomic on the tail and written after; every entry starts as */
+/* Queues: positions are taken with an atomic on the tail and written after; every entry starts as */
 /* -1, so a worker that claimed a position not yet written waits for it (briefly: the writer is    */
 /* between two instructions).  Stores of a node's time and of its queue entries are ordered by     */
-/* __threadfence_block before the counters that publish them.                                     */
-/*                                                                                                 */
-/* Quiescence: a worker with nothing to claim counts itself idle.  When every worker is idle and   */
-/* the queue is empty and stays so (tail read before and after the idle count), no node is in      */
-/* flight and none can become ready; if points were put aside for an inherited stencil state, one  */
-/* worker (elected with a lock, the test repeated under it) resolves the first of them.  Every     */
-/* wait is bounded: a worker idle for FD_WAIT_CYCLES without progress sets the station's status    */
-/* and all workers leave the walk.                                                                  */
+/* __threadfence_block before the counters that publish them.  Every wait is bounded: a worker     */
+/* idle for FD_WAIT_CYCLES without progress sets the station's status and all workers leave the   */
+/* walk; all idle with nothing queued and nodes left is reported the same way.                    */
 
 #define NB_PAD 19                    /* context row stride: the 32 rows fall on distinct banks */
 #define FD_WAIT_CYCLES (4ll << 30)   /* about 2 s at the maximum SM clock */
-#ifndef FD_FACE_WARPS
-#define FD_FACE_WARPS FD_WARPS       /* workers that take part in a face walk */
-#endif
 #define FD_QSPIN (1 << 22)           /* polls of an unwritten queue entry before giving up */
+#define FD_KEYED 0x80000000u         /* counter word: the node's sort key is final */
 
 #define FD_DESC_ROW(F)                                                                              \
     make_desc<F>(0), make_desc<F>(1), make_desc<F>(2), make_desc<F>(3), make_desc<F>(4), make_desc<F>(5), \
@@ -249,9 +251,9 @@ __device__ __forceinline__ int kind_of(int K)
     return K < TK_NE0 ? 0 : K < TK_2D0 ? 1 : K < TK_NF ? 2 : K < TK_1D0 ? 3 : 4;
 }
 
-/* shared by the CTA: the current face's trial descriptors */
+/* shared by the CTA: the trial descriptors of all six faces */
 struct CtaSmem {
-    TrialDesc desc[FDN_NTRIAL];
+    TrialDesc desc[FDN_NFACE][FDN_NTRIAL];
 };
 constexpr int kCtaSmemBytes = (int)((sizeof(CtaSmem) + 15) & ~(size_t)15);
 
@@ -340,16 +342,6 @@ struct Rect {
     int u, v, nu, nv, ulo, uhi, vlo, vhi;
 };
 
-__device__ __forceinline__ Rect rect_of(const Shared &sh, int i)
-{
-    Rect r;
-    r.u = sh.ulo + i % sh.nuf;
-    r.v = sh.vlo + i / sh.nuf;
-    r.nu = sh.nu; r.nv = sh.nv;
-    r.ulo = sh.ulo; r.uhi = sh.uhi; r.vlo = sh.vlo; r.vhi = sh.vhi;
-    return r;
-}
-
 template <int F>
 __device__ __forceinline__ bool any_corner(const float *t18, const Rect &r)
 {
@@ -419,12 +411,12 @@ __device__ __forceinline__ int push_items(unsigned short *items, int n, unsigned
 
 /* evaluate items[0..n) with the warp's lanes; a 2-D value is stored after the causality selection
  * against its floor, which includes the stencil state entering the 2-D block (src/sphfd.c:6116-6121) */
-__device__ void eval_items(const fd_station_dev &sd, const CtaSmem &cs, WarpSmem &ws, int n, int lane, Counters &cn)
+__device__ void eval_items(const fd_station_dev &sd, const TrialDesc *dsc, WarpSmem &ws, int n, int lane, Counters &cn)
 {
     for (int j = lane; j < n; j += 32) {
         const unsigned it = ws.items[j];
         const int slot = (int)(it >> 5), K = (int)(it & 31);
-        const TrialDesc &d = cs.desc[K];
+        const TrialDesc &d = dsc[K];
         const int z = ws.z[slot], y = ws.y[slot];
         const float *t18 = ws.t[slot], *s18 = ws.s[slot];
         const int kind = kind_of(K);
@@ -458,7 +450,7 @@ __device__ void eval_items(const fd_station_dev &sd, const CtaSmem &cs, WarpSmem
  * 2-D block): the running minimum entering the 2-D block — an upper bound for every 2-D trial's
  * turn — and the stale (t0,t4) those trials test against.  Returns the 2-D trials that can still
  * lower the minimum. */
-__device__ unsigned stale_pair(const CtaSmem &cs, WarpSmem &ws, int slot, unsigned gm, unsigned em, float it0,
+__device__ unsigned stale_pair(const TrialDesc *dsc, WarpSmem &ws, int slot, unsigned gm, unsigned em, float it0,
                                float it4)
 {
     const float *t18 = ws.t[slot];
@@ -466,8 +458,8 @@ __device__ unsigned stale_pair(const CtaSmem &cs, WarpSmem &ws, int slot, unsign
     float s0 = it0, s4 = it4;
     for (int K = 0; K < TK_NE0; K++) {
         if (!((gm >> K) & 1u)) continue;
-        s0 = t18[cs.desc[K].slot[0]];
-        s4 = t18[cs.desc[K].slot[4]];
+        s0 = t18[dsc[K].slot[0]];
+        s4 = t18[dsc[K].slot[4]];
         if ((em >> K) & 1u) {
             const double v = ws.res[slot][K];
             if (lt(v, g1)) g1 = v;
@@ -476,8 +468,8 @@ __device__ unsigned stale_pair(const CtaSmem &cs, WarpSmem &ws, int slot, unsign
     const bool gate = lt(1.0e9, g1);
     for (int K = TK_NE0; K < TK_2D0; K++) {
         if (!gate || !((gm >> K) & 1u)) continue;
-        s0 = t18[cs.desc[K].slot[0]];
-        s4 = t18[cs.desc[K].slot[4]];
+        s0 = t18[dsc[K].slot[0]];
+        s4 = t18[dsc[K].slot[4]];
         if ((em >> K) & 1u) {
             const double v = ws.res[slot][K];
             if (lt(v, g1)) g1 = v;
@@ -489,7 +481,7 @@ __device__ unsigned stale_pair(const CtaSmem &cs, WarpSmem &ws, int slot, unsign
     unsigned add = 0;
     for (int K = TK_2D0; K < TK_NF; K++) {
         if (!((gm >> K) & 1u)) continue;
-        const TrialDesc &d = cs.desc[K];
+        const TrialDesc &d = dsc[K];
         const float fl = fmaxf(fmaxf(fmaxf(t18[d.slot[1]], t18[d.slot[2]]), fmaxf(t18[d.slot[3]], s0)), s4);
         if (!prunable(fl, g1)) add |= 1u << K;
     }
@@ -500,7 +492,7 @@ __device__ unsigned stale_pair(const CtaSmem &cs, WarpSmem &ws, int slot, unsign
  * running minimum entering the 2-D block (kept in res[slot][TK_NF]); their value is recorded as the
  * rejection value, which leaves the minimum and the head-wave test as the true value would.
  * Compacts items[0..n) in place and returns the number left. */
-__device__ int filter_2d(const fd_station_dev &sd, const CtaSmem &cs, WarpSmem &ws, int n, int lane)
+__device__ int filter_2d(const fd_station_dev &sd, const TrialDesc *dsc, WarpSmem &ws, int n, int lane)
 {
     int out = 0;
     for (int j0 = 0; j0 < n; j0 += 32) {
@@ -510,7 +502,7 @@ __device__ int filter_2d(const fd_station_dev &sd, const CtaSmem &cs, WarpSmem &
         if (j < n) {
             it = ws.items[j];
             const int slot = (int)(it >> 5), K = (int)(it & 31);
-            const TrialDesc &d = cs.desc[K];
+            const TrialDesc &d = dsc[K];
             const float *t18 = ws.t[slot];
             const float fl = fmaxf(fmaxf(fmaxf(t18[d.slot[1]], t18[d.slot[2]]), fmaxf(t18[d.slot[3]], ws.s0[slot])),
                                    ws.s4[slot]);
@@ -528,47 +520,29 @@ __device__ int filter_2d(const fd_station_dev &sd, const CtaSmem &cs, WarpSmem &
 }
 
 /* ---------------------------------------------------------------------------------------------- */
-/* plane-pipelined sweeps                                                                          */
-/*                                                                                                 */
-/* After a restart the box is one whole model wall and a sweep is a run of full planes, each one's */
-/* inner layer being the previous plane (src/sphfd.c:5623-5674).  A point of plane p+1 needs only  */
-/* the 3x3 block below it in plane p and its earlier neighbours in its own plane; so the planes    */
-/* are walked as one dependency graph instead of one after the other.  Every node has one counter  */
-/* word: inner-layer nodes pending in bits 0-7, in-plane neighbours pending in bits 8-15.  When a   */
-/* node's inner block is complete, the keys of its in-plane neighbours (their inner-layer times)   */
-/* are final, so it learns which neighbours come later and drops them from its count; earlier      */
-/* neighbours drop themselves when they finish.  The word reaching zero queues the node.  The run */
-/* is taken only when no point can need an earlier point's stencil state (see fd_solve).          */
+/* node addressing                                                                                 */
 
 __device__ __forceinline__ unsigned long long node_key(float tin, int i)
 {
     return ((unsigned long long)okey32(tin) << 32) | (unsigned)i;
 }
 
-/* earlier-neighbour byte of fill index i, keys from the inner-layer field at `inner_layer` */
-__device__ unsigned earlier_mask(const fd_station_dev &sd, const Shared &sh, int i, int inner_layer)
+/* grid extent and node strides of the time field and of the slowness model along an axis */
+__device__ __forceinline__ int axis_len(const fd_station_dev &sd, int a) { return a == 0 ? sd.g.nx : a == 1 ? sd.g.ny : sd.g.nz; }
+__device__ __forceinline__ long long t_stride(const fd_station_dev &sd, int a)
 {
-    const fdn_frame fr = frame_of(sh.face);
-    const int nvf = sh.n / sh.nuf, iu = i % sh.nuf, iv = i / sh.nuf;
-    auto tin = [&](int ju, int jv) {
-        int xyz[3];
-        xyz[fr.axis_u] = sh.ulo + ju;
-        xyz[fr.axis_v] = sh.vlo + jv;
-        xyz[fr.axis_n] = inner_layer;
-        return vload(sd.T[((long long)xyz[2] * sd.g.ny + xyz[1]) * sd.g.nx + xyz[0]]);
-    };
-    const unsigned long long ki = node_key(tin(iu, iv), i);
-    unsigned em = 0;
-#pragma unroll
-    for (int k = 0; k < 8; k++) {
-        int du, dv;
-        nb_off(k, du, dv);
-        const int ju = iu + du, jv = iv + dv;
-        if (ju < 0 || ju >= sh.nuf || jv < 0 || jv >= nvf) continue;
-        if (node_key(tin(ju, jv), jv * sh.nuf + ju) < ki) em |= 1u << k;
-    }
-    return em;
+    return a == 0 ? 1ll : a == 1 ? (long long)sd.g.nx : (long long)sd.g.nx * sd.g.ny;
 }
+__device__ __forceinline__ long long s_stride(const fd_station_dev &sd, int a) { return a == 0 ? 1ll : a == 1 ? sd.s_sy : sd.s_sz; }
+
+/* where a node sits: grid index, coordinates, face rectangle, fill index */
+struct Where {
+    long long p;
+    int xyz[3];
+    int i;       /* fill index in its face (instance) */
+    int inst;    /* face instance of a sweep graph, -1 in a face walk */
+    Rect r;
+};
 
 /* append e to a queue with tail counter `tail`; a position past the capacity (a node queued more
  * often than the walk allows) is refused */
@@ -581,56 +555,8 @@ __device__ __forceinline__ void enqueue_to(int *queue, int &tail, int cap, Share
         atomicCAS(&sh.status, 0, 10);
 }
 
-__device__ __forceinline__ void enqueue(int *queue, Shared &sh, int e) { enqueue_to(queue, sh.qtail, sh.qcap, sh, e); }
-
-/* node (plane pp, fill index i) is final: record (last plane), release its later in-plane
- * neighbours and the plane pp+1 nodes whose inner block contains it */
-__device__ void pipelined_release(const fd_station_dev &sd, Shared &sh, int i, int pp, bool writer, float st0,
-                                  float st4, float tin)
-{
-    const int nplane = sh.n, nvf = sh.n / sh.nuf, iu = i % sh.nuf, iv = i / sh.nuf;
-    const fdn_frame fr = frame_of(sh.face);
-    if (pp == sh.np - 1) {
-        if (writer) {
-            sd.scr.rec[i] = make_float2(st0, st4);
-            atomicMax(&sh.exitkey, node_key(tin, i));
-        } else {
-            sd.scr.rec[i] = make_float2(__int_as_float(0x7fc00000), __int_as_float(0x7fc00000));
-        }
-    }
-    __threadfence_block();
-    const long long base = (long long)pp * nplane;
-    unsigned later = inrect_mask(iu, iv, sh.nuf, nvf) & ~(unsigned)sd.scr.pemask[base + i];
-    while (later) {
-        const int k = __ffs(later) - 1;
-        later &= later - 1;
-        int du, dv;
-        nb_off(k, du, dv);
-        const int j = (iv + dv) * sh.nuf + iu + du;
-        const unsigned old = atomicSub(&sd.scr.pcount[base + j], 1u << 8);
-        if (old == (1u << 8)) enqueue(sd.scr.pqueue, sh, (int)(base + j));
-    }
-    if (pp + 1 < sh.np) {
-        const long long nb = base + nplane;
-        const int layer = sh.player0 - pp * fr.inner;   /* this plane = the next plane's inner layer */
-        for (int dv = -1; dv <= 1; dv++)
-            for (int du = -1; du <= 1; du++) {
-                const int ju = iu + du, jv = iv + dv;
-                if (ju < 0 || ju >= sh.nuf || jv < 0 || jv >= nvf) continue;
-                const int j = jv * sh.nuf + ju;
-                const unsigned old = atomicSub(&sd.scr.pcount[nb + j], 1u);
-                if ((old & 0xFFu) != 1u) continue;
-                /* inner block of node j complete: its in-plane order is now known */
-                const unsigned em = earlier_mask(sd, sh, j, layer);
-                sd.scr.pemask[nb + j] = (unsigned char)em;
-                __threadfence_block();
-                const unsigned lat = (unsigned)__popc(inrect_mask(ju, jv, sh.nuf, nvf) & ~em);
-                const unsigned w = old - 1u;
-                const unsigned prev = lat ? atomicSub(&sd.scr.pcount[nb + j], lat << 8) : w;
-                if (prev - (lat << 8) == 0u) enqueue(sd.scr.pqueue, sh, (int)(nb + j));
-            }
-    }
-}
+/* ---------------------------------------------------------------------------------------------- */
+/* face walks (one face at a time; used when the sweep-graph arrays are not available)             */
 
 /* face walk: node i is final; mark it done and release its later in-face neighbours */
 __device__ void face_release(const fd_station_dev &sd, Shared &sh, unsigned char *dag, int i, bool writer,
@@ -658,9 +584,317 @@ __device__ void face_release(const fd_station_dev &sd, Shared &sh, unsigned char
         const int j = (iv + dv) * sh.nuf + iu + du;
         const unsigned sh8 = (j & 3) * 8;
         const unsigned old = atomicSub(reinterpret_cast<unsigned *>(dag) + (j >> 2), 1u << sh8);
-        if (((old >> sh8) & 0xFFu) == 1u) enqueue(sd.scr.queue, sh, j);
+        if (((old >> sh8) & 0xFFu) == 1u) enqueue_to(sd.scr.queue, sh.qtail[0], sh.qcap[0], sh, j);
     }
 }
+
+__device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long x)
+{
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long y = __shfl_xor_sync(0xffffffffu, x, o);
+        x = y > x ? y : x;
+    }
+    return x;
+}
+
+/* ---------------------------------------------------------------------------------------------- */
+/* sweep graphs                                                                                    */
+/*                                                                                                 */
+/* A whole sweep runs as one dependency graph.  Which face instance (a face at one wall position)  */
+/* computes which node depends only on the walls, not on times, so the sweep's schedule of face    */
+/* instances is simulated first; a node's owner then follows from two small shared-memory tables  */
+/* (the instance of each face at each layer, and each instance's rectangle).  A node reads its     */
+/* own-plane 3x3 block and the 3x3 block of its inner layer.  For each pair of nodes where one     */
+/* reads the other and their owners differ, the earlier-owned one must finish first: the reader    */
+/* needs its new value, or it must read the other's old one.  Within one face instance the order   */
+/* is the sort order of the inner-layer times, known once a node's inner block is final (its inner */
+/* block holds the inner nodes of all its in-face neighbours).  Every node keeps one counter word: */
+/* inner block pending (bits 0-7), same-instance neighbours pending (8-15), other-instance nodes    */
+/* pending (16-23), a point waits on it (bit 29), done (bit 30), key final (bit 31).  After a      */
+/* restart (one face) this is a plane pipeline; in the forward sweep it lets all six faces and     */
+/* successive wall positions advance together.                                                     */
+/*                                                                                                 */
+/* Inherited stencil state: a point whose 2-D trials need the state an earlier point left, and    */
+/* whose result depends on it, waits for the last point before it (in the reference's order) that  */
+/* made a writer call: the predecessor by key in its own instance once all keys there are final,   */
+/* else the last writer of the nearest earlier instance once that instance is complete.  Waits    */
+/* are registered on a point (a wait pair and the counter's wait bit) or on an instance event (all */
+/* keys final, all points done; a parked-point entry).                                            */
+
+#define FD_LMAX 1024                 /* largest grid extent a sweep graph handles */
+#ifndef FD_GRAPH_FORWARD
+#define FD_GRAPH_FORWARD 1           /* the first sweep as a graph too */
+#endif
+#define FD_IMAX 3088                 /* face instances: at most nx + ny + nz + 8 */
+#define FD_WAITB 0x20000000u
+#define FD_DONEB 0x40000000u
+
+struct GRect {
+    short face, layer, ulo, uhi, vlo, vhi, nuf, pad;
+};
+
+/* in the dynamic shared memory after the warp areas (the face walks' dependency bytes otherwise) */
+struct GraphSmem {
+    short lay2inst[FDN_NFACE][FD_LMAX];   /* instance of face f at layer l, -1 if none */
+    GRect rect[FD_IMAX];
+};
+
+__device__ __forceinline__ GraphSmem &gsmem(const Shared &sh) { return *reinterpret_cast<GraphSmem *>(sh.gsm); }
+
+/* Neighbour offsets (dx,dy,dz) are numbered k = (dz+1)*9 + (dy+1)*3 + (dx+1), 13 being the node
+ * itself; the opposite offset is 26 - k.  An owner word holds (face << 24) | instance, -1 for a
+ * node no instance of the sweep computes. */
+__device__ __forceinline__ int own_inst(int w) { return w & 0xFFFFFF; }
+__device__ __forceinline__ int own_face(int w) { return w >> 24; }
+
+/* masks of the offsets a node of face f reads (own plane and inner plane) and of its inner plane */
+__device__ void relation_masks(int f, unsigned &ctx, unsigned &inn)
+{
+    const fdn_frame fr = frame_of(f);
+    ctx = 0;
+    inn = 0;
+    for (int k = 0; k < 27; k++) {
+        if (k == 13) continue;
+        const int o[3] = {k % 3 - 1, (k / 3) % 3 - 1, k / 9 - 1};
+        const int on = o[fr.axis_n];
+        if (on == 0 || on == fr.inner) ctx |= 1u << k;
+        if (on == fr.inner) inn |= 1u << k;
+    }
+}
+
+__device__ __forceinline__ int rect_n(const GRect &r) { return r.nuf * (r.vhi - r.vlo + 1); }
+
+/* owner word of node (x,y,z), which must lie in the grid */
+__device__ __forceinline__ int owner_of(const GraphSmem &gs, unsigned faces, int x, int y, int z)
+{
+    const int c[3] = {x, y, z};
+#pragma unroll
+    for (int f = 0; f < 6; f++) {
+        if (!((faces >> f) & 1u)) continue;
+        const fdn_frame fr = frame_of(f);
+        const int I = gs.lay2inst[f][c[fr.axis_n]];
+        if (I < 0) continue;
+        const GRect &r = gs.rect[I];
+        const int u = c[fr.axis_u], v = c[fr.axis_v];
+        if (u >= r.ulo && u <= r.uhi && v >= r.vlo && v <= r.vhi) return (f << 24) | I;
+    }
+    return -1;
+}
+
+/* node index of point j of instance r */
+__device__ __forceinline__ long long inst_node(const fd_station_dev &sd, const GRect &r, int j)
+{
+    const fdn_frame fr = frame_of(r.face);
+    int xyz[3];
+    xyz[fr.axis_u] = r.ulo + j % r.nuf;
+    xyz[fr.axis_v] = r.vlo + j / r.nuf;
+    xyz[fr.axis_n] = r.layer;
+    return ((long long)xyz[2] * sd.g.ny + xyz[1]) * sd.g.nx + xyz[0];
+}
+
+/* sort key of point j of instance r: time of its inner-layer node, then fill index */
+__device__ __forceinline__ unsigned long long inst_key(const fd_station_dev &sd, const GRect &r, int j)
+{
+    const fdn_frame fr = frame_of(r.face);
+    const long long p = inst_node(sd, r, j) + fr.inner * t_stride(sd, fr.axis_n);
+    return node_key(vload(sd.T[p]), j);
+}
+
+/* fill index of node xyz in instance r */
+__device__ __forceinline__ int inst_fill(const GRect &r, const int xyz[3])
+{
+    const fdn_frame fr = frame_of(r.face);
+    return (xyz[fr.axis_v] - r.vlo) * r.nuf + (xyz[fr.axis_u] - r.ulo);
+}
+
+/* points parked on instance I's event `kind` (1: all keys final, 2: all done) go to the resume queue */
+__device__ void fire_event(const fd_station_dev &sd, Shared &sh, int I, int kind)
+{
+    __threadfence_block();
+    if (!(vload(sd.scr.ginst[I].evwait) & kind)) return;
+    const int st = (kind << 24) | I;
+    const int np = min(vload(sh.npark), FD_GPARK_CAP);
+    for (int k = 0; k < np; k++) {
+        if (vload(sd.scr.gpark[k].y) == st && atomicCAS(&sd.scr.gpark[k].y, st, -2) == st) {
+            __threadfence_block();
+            enqueue_to(sd.scr.grq, sh.rqtail, sh.rqcap, sh, vload(sd.scr.gpark[k].x));
+        }
+    }
+}
+
+/* Key event of node j of instance I (its inner block is final): its earlier same-instance
+ * neighbours, recorded, and the later ones dropped from its counter.  Returns the counter word
+ * after the update. */
+__device__ unsigned key_event(const fd_station_dev &sd, Shared &sh, int I, int j, long long q)
+{
+    const GRect &r = gsmem(sh).rect[I];
+    const fdn_frame fr = frame_of(r.face);
+    const int n = rect_n(r), nvf = r.vhi - r.vlo + 1, iv = j / r.nuf, iu = j - iv * r.nuf;
+    const long long su = t_stride(sd, fr.axis_u), sv = t_stride(sd, fr.axis_v);
+    const long long qin = q + fr.inner * t_stride(sd, fr.axis_n);   /* q's inner-layer node */
+    const unsigned inr = inrect_mask(iu, iv, r.nuf, nvf);
+    /* the inner-layer times of q and of its in-rectangle neighbours, all loads issued together */
+    float tn[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        int du, dv;
+        nb_off(k, du, dv);
+        tn[k] = ((inr >> k) & 1u) ? vload(sd.T[qin + du * su + dv * sv]) : 0.f;
+    }
+    const unsigned long long kj = node_key(vload(sd.T[qin]), j);
+    unsigned em = 0;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        int du, dv;
+        nb_off(k, du, dv);
+        if (((inr >> k) & 1u) && node_key(tn[k], j + du + dv * r.nuf) < kj) em |= 1u << k;
+    }
+    sd.scr.gemask[q] = (unsigned char)em;
+    __threadfence_block();
+    const unsigned lat = (unsigned)__popc(inr & ~em);
+    const unsigned add = FD_KEYED - (lat << 8);
+    const unsigned nw = atomicAdd(&sd.scr.gcnt[q], add) + add;
+    if (!sh.nodefer && atomicAdd(&sd.scr.ginst[I].nkeyed, 1) == n - 1) fire_event(sd, sh, I, 1);
+    return nw;
+}
+
+__device__ __forceinline__ bool ready_word(unsigned w) { return (w & ~FD_WAITB) == FD_KEYED; }
+
+__device__ __forceinline__ void graph_ready(const fd_station_dev &sd, Shared &sh, int face, long long q)
+{
+    enqueue_to(sd.scr.gqueue + sh.qbase[face], sh.qtail[face], sh.qcap[face], sh, (int)q);
+}
+
+/* drop one inner-block (inner) or other-instance dependency of node q (instance oq, face fq) */
+__device__ __forceinline__ void graph_dec(const fd_station_dev &sd, Shared &sh, long long q, int oq, int fq,
+                                          const int qxyz[3], bool inner)
+{
+    const unsigned dec = inner ? 1u : (1u << 16);
+    const unsigned nw = atomicSub(&sd.scr.gcnt[q], dec) - dec;
+    if (inner && (nw & 0xFFu) == 0u) {
+        /* q's inner block is complete: its key and in-face order are now known */
+        if (ready_word(key_event(sd, sh, oq, inst_fill(gsmem(sh).rect[oq], qxyz), q))) graph_ready(sd, sh, fq, q);
+    } else if (ready_word(nw)) {
+        graph_ready(sd, sh, fq, q);
+    }
+}
+
+/* node p (instance I, face F, fill index i) is final: record, release what waits on it */
+__device__ void graph_release(const fd_station_dev &sd, Shared &sh, int F, long long p, const int pxyz[3], int I, int i,
+                              bool writer, float st0, float st4, float tin)
+{
+    const GraphSmem &gs = gsmem(sh);
+    const GRect &r = gs.rect[I];
+    fd_ginst &gi = sd.scr.ginst[I];
+    /* records: of every point when a point may need an earlier one's; else only the last instance's,
+     * for the state the sweep leaves */
+    if (!sh.nodefer || I == sh.ninst - 1) {
+        if (writer) {
+            sd.scr.grec[p] = make_float2(st0, st4);
+            atomicMax(&gi.exitkey, node_key(tin, i));
+        } else {
+            sd.scr.grec[p] = make_float2(__int_as_float(0x7fc00000), __int_as_float(0x7fc00000));
+        }
+    }
+    __threadfence_block();
+    /* done; a point waiting for the stencil state left before it resumes its search */
+    if (!sh.nodefer && (atomicOr(&sd.scr.gcnt[p], FD_DONEB) & FD_WAITB)) {
+        __threadfence_block();
+        const int nw = min(vload(sh.nwait), FD_GWAIT_CAP);
+        for (int k = 0; k < nw; k++)
+            if (vload(sd.scr.gwait[k].x) == (int)p && atomicCAS(&sd.scr.gwait[k].x, (int)p, -1) == (int)p)
+                enqueue_to(sd.scr.grq, sh.rqtail, sh.rqcap, sh, vload(sd.scr.gwait[k].y));
+    }
+    const int nx = sd.g.nx, ny = sd.g.ny;
+    const int x = pxyz[0], y = pxyz[1], z = pxyz[2];
+    const fdn_frame fr = frame_of(F);
+    if (sh.single) {
+        /* one face: the next instance's nodes whose inner block holds p */
+        if (I + 1 < sh.ninst && gs.rect[I + 1].layer == r.layer - fr.inner) {
+            const GRect &rn = gs.rect[I + 1];
+            int c[3] = {x, y, z};
+            c[fr.axis_n] = rn.layer;
+            const int u0 = c[fr.axis_u], v0 = c[fr.axis_v];
+            for (int dv = -1; dv <= 1; dv++)
+                for (int du = -1; du <= 1; du++) {
+                    const int u = u0 + du, v = v0 + dv;
+                    if (u < rn.ulo || u > rn.uhi || v < rn.vlo || v > rn.vhi) continue;
+                    int qxyz[3];
+                    qxyz[fr.axis_u] = u;
+                    qxyz[fr.axis_v] = v;
+                    qxyz[fr.axis_n] = rn.layer;
+                    const long long q = ((long long)qxyz[2] * ny + qxyz[1]) * nx + qxyz[0];
+                    graph_dec(sd, sh, q, I + 1, F, qxyz, true);
+                }
+        }
+    } else {
+        /* nodes of later instances that read p, or that p read */
+        const unsigned myctx = sh.ctxm[F];
+        for (int k = 0; k < 27; k++) {
+            if (k == 13) continue;
+            const int qxyz[3] = {x + k % 3 - 1, y + (k / 3) % 3 - 1, z + k / 9 - 1};
+            if (qxyz[0] < 0 || qxyz[0] >= nx || qxyz[1] < 0 || qxyz[1] >= ny || qxyz[2] < 0 || qxyz[2] >= sd.g.nz)
+                continue;
+            const int w = owner_of(gs, sh.gfaces, qxyz[0], qxyz[1], qxyz[2]);
+            if (w < 0 || own_inst(w) <= I) continue;
+            const int fq = own_face(w);
+            if (!((myctx >> k) & 1u) && !((sh.ctxm[fq] >> (26 - k)) & 1u)) continue;
+            const long long q = ((long long)qxyz[2] * ny + qxyz[1]) * nx + qxyz[0];
+            graph_dec(sd, sh, q, own_inst(w), fq, qxyz, (sh.innm[fq] >> (26 - k)) & 1u);
+        }
+    }
+    /* later neighbours in the same instance */
+    const int nvf = r.vhi - r.vlo + 1, iu = i % r.nuf, iv = i / r.nuf;
+    unsigned later = inrect_mask(iu, iv, r.nuf, nvf) & ~(unsigned)sd.scr.gemask[p];
+    while (later) {
+        const int k = __ffs(later) - 1;
+        later &= later - 1;
+        int du, dv;
+        nb_off(k, du, dv);
+        const long long q = p + du * t_stride(sd, fr.axis_u) + dv * t_stride(sd, fr.axis_v);
+        const unsigned nw = atomicSub(&sd.scr.gcnt[q], 1u << 8) - (1u << 8);
+        if (ready_word(nw)) graph_ready(sd, sh, F, q);
+    }
+}
+
+/* point w waits for an event of instance I (kind 1: all keys final, 2: all points done) (lane 0) */
+__device__ void wait_event(const fd_station_dev &sd, Shared &sh, int w, int I, int kind)
+{
+    const int k = atomicAdd(&sh.npark, 1);
+    if (k >= FD_GPARK_CAP) {
+        atomicCAS(&sh.status, 0, 15);
+        return;
+    }
+    const int st = (kind << 24) | I;
+    sd.scr.gpark[k].x = w;
+    __threadfence_block();
+    atomicExch(&sd.scr.gpark[k].y, st);
+    atomicOr(&sd.scr.ginst[I].evwait, kind);
+    __threadfence_block();
+    const int n = rect_n(gsmem(sh).rect[I]);
+    const bool now = kind == 1 ? vload(sd.scr.ginst[I].nkeyed) >= n : vload(sd.scr.ginst[I].ndone) >= n;
+    if (now && atomicCAS(&sd.scr.gpark[k].y, st, -2) == st) enqueue_to(sd.scr.grq, sh.rqtail, sh.rqcap, sh, w);
+}
+
+/* point w waits for point p to be done (lane 0).  Returns false if p is already done (no wait). */
+__device__ bool wait_point(const fd_station_dev &sd, Shared &sh, int w, long long p)
+{
+    const int k = atomicAdd(&sh.nwait, 1);
+    if (k >= FD_GWAIT_CAP) {
+        atomicCAS(&sh.status, 0, 15);
+        return true;
+    }
+    sd.scr.gwait[k].y = w;
+    __threadfence_block();
+    atomicExch(&sd.scr.gwait[k].x, (int)p);
+    __threadfence_block();
+    if (!(atomicOr(&sd.scr.gcnt[p], FD_WAITB) & FD_DONEB)) return true;
+    /* p finished meanwhile: take the pair back unless p's release already took it (and queued w) */
+    return atomicCAS(&sd.scr.gwait[k].x, (int)p, -1) != (int)p;
+}
+
+/* ---------------------------------------------------------------------------------------------- */
+/* evaluation of one chunk                                                                         */
 
 /* The reference's sequential minimum over the 22 trials of one node, from the values computed
  * by the warp (new-edge and new-face values that were not precomputed are evaluated here — they
@@ -672,8 +906,8 @@ __device__ void face_release(const fd_station_dev &sd, Shared &sh, unsigned char
  * stale floor can only turn a 2-D value into the rejection value, so if no 2-D value lowered
  * the running minimum the result is the one the true state gives and the node commits; else it
  * returns false without committing. */
-__device__ bool commit_node(const fd_station_dev &sd, Shared &sh, const CtaSmem &cs, WarpSmem &ws, int slot, int i,
-                            int pp, long long pT, unsigned gm, unsigned em, float it0, float it4, bool permissive,
+__device__ bool commit_node(const fd_station_dev &sd, Shared &sh, const TrialDesc *dsc, WarpSmem &ws, int slot,
+                            int F, const Where &wh, unsigned gm, unsigned em, float it0, float it4, bool permissive,
                             unsigned char *dag, Counters &cn)
 {
     const float *t18 = ws.t[slot], *s18 = ws.s[slot];
@@ -690,7 +924,7 @@ __device__ bool commit_node(const fd_station_dev &sd, Shared &sh, const CtaSmem 
         /* the first-contact tests are made on entry to their blocks (src/sphfd.c:1375, :1698) */
         if (K == TK_NE0 || K == TK_NF) gate = lt(1.0e9, guess);
         if (!((gm >> K) & 1u)) continue;
-        const TrialDesc &d = cs.desc[K];
+        const TrialDesc &d = dsc[K];
         const bool ev = (em >> K) & 1u;
         double v;
         if (K < TK_2D0 || K == TK_NF) {
@@ -723,67 +957,102 @@ __device__ bool commit_node(const fd_station_dev &sd, Shared &sh, const CtaSmem 
     }
     if (permissive && win2d) return false;
     if (lt(guess, told)) {
-        sd.T[pT] = __double2float_rn(guess);
+        sd.T[wh.p] = __double2float_rn(guess);
         if (lastK >= 0) {
             /* only the last head trial that lowered the minimum sets the measure that is tested */
-            const double fhead = (last_gb - last_v) / head_den(cs.desc[lastK], s18, sd.g, z, y);
-            if (fhead > FD_HEADTEST) atomicAdd(&sh.headw[frame_of(sh.face).headw], 1);
+            const double fhead = (last_gb - last_v) / head_den(dsc[lastK], s18, sd.g, z, y);
+            if (fhead > FD_HEADTEST) atomicAdd(&sh.headw[frame_of(F).headw], 1);
         }
     }
-    if (sh.pipelined)
-        pipelined_release(sd, sh, i, pp, writers != 0, st0, st4, t18[13]);
+    if (sh.graph)
+        graph_release(sd, sh, F, wh.p, wh.xyz, wh.inst, wh.i, writers != 0, st0, st4, t18[13]);
     else
-        face_release(sd, sh, dag, i, writers != 0, st0, st4);
+        face_release(sd, sh, dag, wh.i, writers != 0, st0, st4);
     return true;
 }
 
-/* Evaluate and commit one chunk: lane l holds queue entry e (-1 for none).  A node given with
- * have_inherit uses (it0, it4) as the stencil state entering it.  All 32 lanes call. */
-__device__ void warp_chunk(const fd_station_dev &sd, Shared &sh, const CtaSmem &cs, WarpSmem &ws, int e,
+/* where the node of queue entry e lies: a fill index in a face walk, a grid index in a graph;
+ * ok false for a graph node no instance owns */
+__device__ __forceinline__ Where locate(const fd_station_dev &sd, const Shared &sh, int F, int e, bool &ok)
+{
+    const fdn_frame fr = frame_of(F);
+    Where wh;
+    ok = true;
+    if (sh.graph) {
+        wh.p = e;
+        const int nx = sd.g.nx, ny = sd.g.ny, exy = e / nx;
+        wh.xyz[0] = e - exy * nx;
+        wh.xyz[2] = exy / ny;
+        wh.xyz[1] = exy - wh.xyz[2] * ny;
+        const int w = owner_of(gsmem(sh), sh.gfaces, wh.xyz[0], wh.xyz[1], wh.xyz[2]);
+        if (w < 0) {
+            ok = false;
+            return wh;
+        }
+        wh.inst = own_inst(w);
+        const GRect &gr = gsmem(sh).rect[wh.inst];
+        wh.r.u = wh.xyz[fr.axis_u];
+        wh.r.v = wh.xyz[fr.axis_v];
+        wh.r.ulo = gr.ulo; wh.r.uhi = gr.uhi; wh.r.vlo = gr.vlo; wh.r.vhi = gr.vhi;
+        wh.i = inst_fill(gr, wh.xyz);
+    } else {
+        wh.i = e;
+        wh.inst = -1;
+        wh.r.u = sh.ulo + e % sh.nuf;
+        wh.r.v = sh.vlo + e / sh.nuf;
+        wh.r.ulo = sh.ulo; wh.r.uhi = sh.uhi; wh.r.vlo = sh.vlo; wh.r.vhi = sh.vhi;
+        wh.xyz[fr.axis_u] = wh.r.u;
+        wh.xyz[fr.axis_v] = wh.r.v;
+        wh.xyz[fr.axis_n] = sh.layer;
+        wh.p = ((long long)wh.xyz[2] * sd.g.ny + wh.xyz[1]) * sd.g.nx + wh.xyz[0];
+    }
+    wh.r.nu = axis_len(sd, fr.axis_u);
+    wh.r.nv = axis_len(sd, fr.axis_v);
+    return wh;
+}
+
+/* Evaluate and commit one chunk of face F: lane l holds queue entry e (-1 for none).  A node given
+ * with have_inherit uses (it0, it4) as the stencil state entering it.  All 32 lanes call. */
+__device__ void warp_chunk(const fd_station_dev &sd, Shared &sh, const CtaSmem &cs, WarpSmem &ws, int F, int e,
                            bool have_inherit, float it0, float it4, unsigned char *dag, Counters &cn)
 {
     const int lane = threadIdx.x & 31;
-    const bool valid = e >= 0;
-    const fdn_frame fr = frame_of(sh.face);
-    int i = 0, pp = -1;
-    long long pT = 0;
+    const fdn_frame fr = frame_of(F);
+    const TrialDesc *dsc = cs.desc[F];
+    Where wh;
     unsigned gm = 0, em = 0;
     bool permissive = false;
     FD_TIC(ta);
-    if (valid) {
-        /* entries: fill indices, or plane * n + fill index in a pipelined sweep */
-        int layer = sh.layer;
-        if (sh.pipelined) {
-            pp = e / sh.n;
-            i = e - pp * sh.n;
-            layer = sh.player0 - pp * fr.inner;
-        } else {
-            i = e;
+    if (e >= 0) {
+        bool ok;
+        wh = locate(sd, sh, F, e, ok);
+        if (!ok) {
+            atomicCAS(&sh.status, 0, 14);   /* a queued node no face instance owns */
+            e = -1;
         }
-        const int u = sh.ulo + i % sh.nuf, v = sh.vlo + i / sh.nuf;
-        int xyz[3];
-        xyz[fr.axis_u] = u;
-        xyz[fr.axis_v] = v;
-        xyz[fr.axis_n] = layer;
-        pT = ((long long)xyz[2] * sd.g.ny + xyz[1]) * sd.g.nx + xyz[0];
-        const long long pS = (long long)xyz[2] * sd.s_sz + (long long)xyz[1] * sd.s_sy + xyz[0];
-        ws.z[lane] = xyz[2];
-        ws.y[lane] = xyz[1];
+    }
+    const bool valid = e >= 0;
+    if (valid) {
+        const long long pS = (long long)wh.xyz[2] * sd.s_sz + (long long)wh.xyz[1] * sd.s_sy + wh.xyz[0];
+        ws.z[lane] = wh.xyz[2];
+        ws.y[lane] = wh.xyz[1];
         float *tr = ws.t[lane], *sr = ws.s[lane];
-        const long long inner_t = (long long)fr.inner * sh.sn, inner_s = (long long)fr.inner * sh.ssn;
+        const long long su = t_stride(sd, fr.axis_u), sv = t_stride(sd, fr.axis_v);
+        const long long ssu = s_stride(sd, fr.axis_u), ssv = s_stride(sd, fr.axis_v);
+        const long long inner_t = fr.inner * t_stride(sd, fr.axis_n), inner_s = fr.inner * s_stride(sd, fr.axis_n);
 #pragma unroll
         for (int nb = 0; nb < NB_N; nb++) {
             const int w = nb / 9, dv = (nb / 3) % 3 - 1, du = nb % 3 - 1;
-            const int uu = u + du, vv = v + dv;
+            const int uu = wh.r.u + du, vv = wh.r.v + dv;
             float tv = 0.f, svv = 0.f;
-            if (uu >= 0 && uu < sh.nu && vv >= 0 && vv < sh.nv) {
-                tv = sd.T[pT + du * sh.su + dv * sh.sv + (w ? inner_t : 0ll)];
-                svv = __ldg(&sd.S[pS + du * sh.ssu + dv * sh.ssv + (w ? inner_s : 0ll)]);
+            if (uu >= 0 && uu < wh.r.nu && vv >= 0 && vv < wh.r.nv) {
+                tv = sd.T[wh.p + du * su + dv * sv + (w ? inner_t : 0ll)];
+                svv = __ldg(&sd.S[pS + du * ssu + dv * ssv + (w ? inner_s : 0ll)]);
             }
             tr[nb] = tv;
             sr[nb] = svv;
         }
-        guards(sh.face, tr, rect_of(sh, i), gm, em);
+        guards(F, tr, wh.r, gm, em);
         /* a 2-D trial before any corner / new-edge call reads the state an earlier point left */
         const double told = f2d(tr[NB_POINT]);
         permissive = !have_inherit && (gm & 0xFu) == 0 && !((gm & 0xF0u) && told > 1.0e9) && (gm & 0xFF00u);
@@ -794,30 +1063,40 @@ __device__ void warp_chunk(const fd_station_dev &sd, Shared &sh, const CtaSmem &
     __syncwarp();
     FD_TOC(1, ta);
     FD_TIC(tb);
-    eval_items(sd, cs, ws, n1, lane, cn);
+    eval_items(sd, dsc, ws, n1, lane, cn);
     __syncwarp();
     const float lo = __int_as_float(0xff800000);   /* -inf: no stale floor */
     const float p0 = permissive ? lo : it0, p4 = permissive ? lo : it4;
-    if (valid) em |= stale_pair(cs, ws, lane, gm, em, p0, p4);
+    if (valid) em |= stale_pair(dsc, ws, lane, gm, em, p0, p4);
     __syncwarp();
     int n2 = push_items(ws.items, 0, em, TK_2D0, TK_NF, lane);
     __syncwarp();
-    n2 = filter_2d(sd, cs, ws, n2, lane);
+    n2 = filter_2d(sd, dsc, ws, n2, lane);
     __syncwarp();
-    eval_items(sd, cs, ws, n2, lane, cn);
+    eval_items(sd, dsc, ws, n2, lane, cn);
     __syncwarp();
     FD_TOC(2, tb);
     FD_TIC(tc);
     bool fin = false;
     if (valid) {
-        fin = commit_node(sd, sh, cs, ws, lane, i, pp, pT, gm, em, p0, p4, permissive, dag, cn);
+        fin = commit_node(sd, sh, dsc, ws, lane, F, wh, gm, em, p0, p4, permissive, dag, cn);
         if (!fin) {
-            if (sh.pipelined) {
-                atomicCAS(&sh.status, 0, 6);   /* excluded by the pipelining precondition */
-            } else {
-                atomicAdd(reinterpret_cast<unsigned long long *>(&sh.deferred), 1ull);
-                enqueue_to(sd.scr.rq, sh.rqtail, sh.rqcap, sh, e);
-            }
+            atomicAdd(reinterpret_cast<unsigned long long *>(&sh.deferred), 1ull);
+            if (sh.nodefer)
+                atomicCAS(&sh.status, 0, 6);   /* excluded by the sweep's precondition */
+            else
+                enqueue_to(sh.graph ? sd.scr.grq : sd.scr.rq, sh.rqtail, sh.rqcap, sh, e);
+        }
+    }
+    if (sh.graph && !sh.nodefer) {
+        /* points done per face instance, one atomic per instance in the chunk; the instance
+         * complete wakes points waiting for its last writer */
+        const int key = fin ? wh.inst : -1;
+        const unsigned peers = __match_any_sync(0xffffffffu, key);
+        if (fin && lane == __ffs(peers) - 1) {
+            const int c = __popc(peers);
+            const int old = atomicAdd(&sd.scr.ginst[key].ndone, c);
+            if (old + c == rect_n(gsmem(sh).rect[key])) fire_event(sd, sh, key, 2);
         }
     }
     const unsigned done = __ballot_sync(0xffffffffu, fin);
@@ -829,16 +1108,10 @@ __device__ void warp_chunk(const fd_station_dev &sd, Shared &sh, const CtaSmem &
     FD_TOC(3, tc);
 }
 
-__device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long x)
-{
-    for (int o = 16; o > 0; o >>= 1) {
-        const unsigned long long y = __shfl_xor_sync(0xffffffffu, x, o);
-        x = y > x ? y : x;
-    }
-    return x;
-}
+/* ---------------------------------------------------------------------------------------------- */
+/* inherited stencil state                                                                         */
 
-/* the face point that precedes point c in sort order (largest key below c's), -1 if none */
+/* face walk: the point that precedes point c in sort order (largest key below c's), -1 if none */
 __device__ int predecessor(const fd_station_dev &sd, int n, int c, int lane)
 {
     const unsigned long long kc = sd.scr.key[c];
@@ -860,8 +1133,8 @@ __device__ int predecessor(const fd_station_dev &sd, int n, int c, int lane)
     return best ? (int)(best & 0xffffffffu) : -1;
 }
 
-/* Point w needs the stencil state left by the last point before it in sort order that made a
- * writer call.  Walk back through the sort order: a done writer gives its record; a done
+/* Face walk: point w needs the stencil state left by the last point before it in sort order that
+ * made a writer call.  Walk back through the sort order: a done writer gives its record; a done
  * non-writer passes the search to its predecessor; a point not yet done takes w as its waiter and
  * queues it again when it finishes (a point has at most one waiter: waiters lie between it and the
  * next pending point).  Before the face's first point the state is the one the face started with.
@@ -879,13 +1152,11 @@ __device__ void resume_waiter(const fd_station_dev &sd, Shared &sh, const CtaSme
             if (p < 0) {
                 verdict = 1;
             } else {
-                int st = vload(sd.scr.pst[p]);
-                if (st != -2) {
+                if (vload(sd.scr.pst[p]) != -2) {
                     const int old = atomicCAS(&sd.scr.pst[p], -1, w);
                     if (old == -1) verdict = 2;
                     else if (old == -2) verdict = 3;
                     else { atomicCAS(&sh.status, 0, 11); verdict = 2; }   /* a second waiter */
-                    st = old;
                 }
                 if (verdict == 0 || verdict == 3) {
                     __threadfence_block();
@@ -900,7 +1171,7 @@ __device__ void resume_waiter(const fd_station_dev &sd, Shared &sh, const CtaSme
         if (verdict == 1) {
             t0 = __shfl_sync(0xffffffffu, t0, 0);
             t4 = __shfl_sync(0xffffffffu, t4, 0);
-            warp_chunk(sd, sh, cs, ws, lane == 0 ? w : -1, true, t0, t4, dag, cn);
+            warp_chunk(sd, sh, cs, ws, sh.face, lane == 0 ? w : -1, true, t0, t4, dag, cn);
             return;
         }
         c = p;
@@ -908,18 +1179,101 @@ __device__ void resume_waiter(const fd_station_dev &sd, Shared &sh, const CtaSme
     if (lane == 0) atomicCAS(&sh.status, 0, 12);
 }
 
-/* nothing queued, every worker idle, and both queues unchanged across the idle count (lane 0) */
+/* Sweep graph: the same search for point w (a grid index), by the reference's order of face
+ * instances and, within one, of keys.  Registers w on an instance event or a point when the
+ * answer is not yet known.  One warp; evaluates w when found. */
+__device__ void resume_graph(const fd_station_dev &sd, Shared &sh, const CtaSmem &cs, WarpSmem &ws, int w,
+                             Counters &cn)
+{
+    const int lane = threadIdx.x & 31;
+    const GraphSmem &gs = gsmem(sh);
+    const int nx = sd.g.nx, ny = sd.g.ny;
+    const int wxy = w / nx;
+    const int xyz[3] = {w - wxy * nx, wxy % ny, wxy / ny};
+    const int ow = owner_of(gs, sh.gfaces, xyz[0], xyz[1], xyz[2]);
+    if (ow < 0) {
+        if (lane == 0) atomicCAS(&sh.status, 0, 14);
+        return;
+    }
+    const int I = own_inst(ow);
+    const GRect &r = gs.rect[I];
+    const int n = rect_n(r);
+    if (vload(sd.scr.ginst[I].nkeyed) < n) {   /* keys below w's not all known yet */
+        if (lane == 0) wait_event(sd, sh, w, I, 1);
+        return;
+    }
+    unsigned long long kc = inst_key(sd, r, inst_fill(r, xyz));
+    for (int guard = 0; guard <= 2 * n + 2; guard++) {
+        /* predecessor in the instance */
+        unsigned long long best = 0ull;
+        for (int j = lane; j < n; j += 32) {
+            const unsigned long long k = inst_key(sd, r, j);
+            if (k < kc && k > best) best = k;
+        }
+        best = warp_max_u64(best);
+        int verdict = 0;   /* 0 continue below best, 1 found, 2 waiting */
+        float t0 = sh.carry_t0, t4 = sh.carry_t4;
+        if (lane == 0) {
+            if (best) {
+                const long long p = inst_node(sd, r, (int)(best & 0xffffffffu));
+                if (!(vload(sd.scr.gcnt[p]) & FD_DONEB) && wait_point(sd, sh, w, p)) {
+                    verdict = 2;
+                } else {
+                    __threadfence_block();
+                    const float r0 = vload(sd.scr.grec[p].x), r4 = vload(sd.scr.grec[p].y);
+                    if (!isnan(r0)) { verdict = 1; t0 = r0; t4 = r4; }
+                }
+            } else {
+                /* no earlier point in the instance: the last writer of an earlier instance */
+                verdict = 1;
+                for (int J = I - 1; J >= 0; J--) {
+                    const GRect &rj = gs.rect[J];
+                    if (vload(sd.scr.ginst[J].ndone) < rect_n(rj)) { wait_event(sd, sh, w, J, 2); verdict = 2; break; }
+                    __threadfence_block();
+                    const unsigned long long ek = vload(sd.scr.ginst[J].exitkey);
+                    if (ek) {
+                        const long long p = inst_node(sd, rj, (int)(ek & 0xffffffffu));
+                        t0 = vload(sd.scr.grec[p].x);
+                        t4 = vload(sd.scr.grec[p].y);
+                        break;
+                    }
+                }
+            }
+        }
+        verdict = __shfl_sync(0xffffffffu, verdict, 0);
+        if (verdict == 2) return;
+        if (verdict == 1) {
+            t0 = __shfl_sync(0xffffffffu, t0, 0);
+            t4 = __shfl_sync(0xffffffffu, t4, 0);
+            warp_chunk(sd, sh, cs, ws, r.face, lane == 0 ? w : -1, true, t0, t4, nullptr, cn);
+            return;
+        }
+        kc = best;
+    }
+    if (lane == 0) atomicCAS(&sh.status, 0, 12);
+}
+
+/* ---------------------------------------------------------------------------------------------- */
+/* the worker loop                                                                                 */
+
+/* nothing queued, every worker idle, and all queues unchanged across the idle count (lane 0) */
 __device__ __forceinline__ bool quiescent(Shared &sh)
 {
-    const int t0 = vload(sh.qtail), h0 = vload(sh.qhead), r0 = vload(sh.rqtail), g0 = vload(sh.rqhead);
-    if (h0 != t0 || r0 != g0) return false;
+    int t0[6], r0 = vload(sh.rqtail);
+    for (int k = 0; k < sh.nq; k++) {
+        t0[k] = vload(sh.qtail[k]);
+        if (vload(sh.qhead[k]) != t0[k]) return false;
+    }
+    if (vload(sh.rqhead) != r0) return false;
     __threadfence_block();
     if (vload(sh.idle) != FD_WARPS) return false;
     __threadfence_block();
-    return vload(sh.qtail) == t0 && vload(sh.qhead) == t0 && vload(sh.rqtail) == r0 && vload(sh.rqhead) == r0;
+    for (int k = 0; k < sh.nq; k++)
+        if (vload(sh.qtail[k]) != t0[k] || vload(sh.qhead[k]) != t0[k]) return false;
+    return vload(sh.rqtail) == r0 && vload(sh.rqhead) == r0;
 }
 
-/* claim one entry of a queue (lane 0): spins briefly for an entry whose writer is between its two
+/* read a claimed queue entry: spins briefly for an entry whose writer is between its two
  * instructions; -1 and a status on failure */
 __device__ __forceinline__ int read_entry(const int *queue, int pos, Shared &sh)
 {
@@ -934,34 +1288,48 @@ __device__ __forceinline__ int read_entry(const int *queue, int pos, Shared &sh)
 }
 
 /* the worker loop of one walk over `total` nodes; all warps call it between two CTA barriers */
-__device__ void run_walk(const fd_station_dev &sd, Shared &sh, const CtaSmem &cs, WarpSmem &ws, int *queue,
-                         int total, unsigned char *dag, Counters &cn)
+__device__ void run_walk(const fd_station_dev &sd, Shared &sh, const CtaSmem &cs, WarpSmem &ws, int total,
+                         unsigned char *dag, Counters &cn)
 {
     const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    int *queue = sh.graph ? sd.scr.gqueue : sd.scr.queue;
+    int *rq = sh.graph ? sd.scr.grq : sd.scr.rq;
     bool idle = false;
     long long since = clock64();
     long long chunks = 0;
     for (;;) {
-        int act = 0, h = 0, m = 0;   /* act: 0 wait, 1 chunk, 2 resume a waiter, 3 leave */
+        int act = 0, h = 0, m = 0, qf = 0;   /* act: 0 wait, 1 chunk, 2 resume a waiter, 3 leave */
         if (lane == 0) {
             if (vload(sh.status) != 0 || vload(sh.ndone) >= total) {
                 act = 3;
             } else {
                 const int rh = vload(sh.rqhead), rt0 = vload(sh.rqtail), rt = rt0 < sh.rqcap ? rt0 : sh.rqcap;
-                const int head = vload(sh.qhead), qt = vload(sh.qtail), tail = qt < sh.qcap ? qt : sh.qcap;
                 if (rh < rt) {
                     if (idle) { atomicSub(&sh.idle, 1); idle = false; }
-                    if (atomicCAS(&sh.rqhead, rh, rh + 1) == rh) { act = 2; h = read_entry(sd.scr.rq, rh, sh); }
-                } else if (head < tail && (sh.pipelined || (int)(threadIdx.x >> 5) < FD_FACE_WARPS)) {
-                    if (idle) { atomicSub(&sh.idle, 1); idle = false; }
-                    const int want = tail - head < 32 ? tail - head : 32;
-                    if (atomicCAS(&sh.qhead, head, head + want) == head) { act = 1; h = head; m = want; }
+                    if (atomicCAS(&sh.rqhead, rh, rh + 1) == rh) { act = 2; h = read_entry(rq, rh, sh); }
                 } else {
-                    if (!idle) { __threadfence_block(); atomicAdd(&sh.idle, 1); idle = true; }
-                    /* all idle with nothing queued and nodes left: nothing can release them */
-                    if (quiescent(sh) && vload(sh.ndone) < total) {
-                        atomicCAS(&sh.status, 0, 3);
-                        act = 3;
+                    /* the fullest queue, starting the scan at a warp-dependent face */
+                    int best = -1, bavail = 0, bhead = 0;
+                    for (int k0 = 0; k0 < sh.nq; k0++) {
+                        const int k = (k0 + warp) % sh.nq;
+                        const int hd = vload(sh.qhead[k]), qt = vload(sh.qtail[k]);
+                        const int tl = qt < sh.qcap[k] ? qt : sh.qcap[k];
+                        if (tl - hd > bavail) { bavail = tl - hd; best = k; bhead = hd; }
+                    }
+                    if (best >= 0) {
+                        if (idle) { atomicSub(&sh.idle, 1); idle = false; }
+                        const int want = bavail < 32 ? bavail : 32;
+                        if (atomicCAS(&sh.qhead[best], bhead, bhead + want) == bhead) {
+                            act = 1; h = sh.qbase[best] + bhead; m = want; qf = best;
+                        }
+                    } else {
+                        if (!idle) { __threadfence_block(); atomicAdd(&sh.idle, 1); idle = true; }
+                        /* all idle with nothing queued and nodes left: nothing can release them */
+                        if (quiescent(sh) && vload(sh.ndone) < total) {
+                            atomicCAS(&sh.status, 0, 3);
+                            act = 3;
+                        }
                     }
                 }
                 if (act == 1 || act == 2) {
@@ -977,6 +1345,7 @@ __device__ void run_walk(const fd_station_dev &sd, Shared &sh, const CtaSmem &cs
         h = __shfl_sync(0xffffffffu, h, 0);
         if (act == 1) {
             m = __shfl_sync(0xffffffffu, m, 0);
+            qf = __shfl_sync(0xffffffffu, qf, 0);
             int e = -1;
             if (lane < m) {
                 const volatile int *q = queue + h + lane;
@@ -988,18 +1357,33 @@ __device__ void run_walk(const fd_station_dev &sd, Shared &sh, const CtaSmem &cs
                 if (e < 0) atomicCAS(&sh.status, 0, 9);   /* a claimed entry never written */
             }
             __threadfence_block();
-            warp_chunk(sd, sh, cs, ws, e, false, 0.f, 0.f, dag, cn);
+            warp_chunk(sd, sh, cs, ws, sh.graph ? qf : sh.face, e, false, 0.f, 0.f, dag, cn);
             chunks++;
             continue;
         }
         if (act == 2) {
             __threadfence_block();
-            if (h >= 0) resume_waiter(sd, sh, cs, ws, h, dag, cn);
+            if (h >= 0) {
+                if (sh.graph)
+                    resume_graph(sd, sh, cs, ws, h, cn);
+                else
+                    resume_waiter(sd, sh, cs, ws, h, dag, cn);
+            }
             continue;
         }
         __nanosleep(64);
     }
     if (lane == 0 && chunks) atomicAdd(reinterpret_cast<unsigned long long *>(&sh.rounds), (unsigned long long)chunks);
+}
+
+/* reset the walk counters (thread 0) */
+__device__ void walk_reset(Shared &sh, int nq, int rqcap)
+{
+    sh.nq = nq;
+    for (int k = 0; k < 6; k++) { sh.qhead[k] = 0; sh.qtail[k] = 0; sh.qcap[k] = 0; sh.qbase[k] = 0; }
+    sh.rqhead = sh.rqtail = sh.idle = sh.ndone = sh.npark = 0;
+    sh.rqcap = rqcap;
+    sh.exitkey = 0ull;
 }
 
 /* Walk the current face (parameters in sh) in dependency order. */
@@ -1013,8 +1397,6 @@ __device__ void face_walk(const fd_station_dev &sd, Shared &sh, CtaSmem &cs, War
     unsigned char *emask = dag + sh.n_pad;
     int *queue = sd.scr.queue;
     FD_TIC(t0);
-    /* trial descriptors of this face */
-    for (int k = tid; k < FDN_NTRIAL; k += blockDim.x) cs.desc[k] = c_desc[sh.face * FDN_NTRIAL + k];
     /* keys: time of the inner-layer neighbour, then fill index */
     for (int i = tid; i < n; i += blockDim.x) {
         int xyz[3];
@@ -1029,10 +1411,9 @@ __device__ void face_walk(const fd_station_dev &sd, Shared &sh, CtaSmem &cs, War
         sd.scr.rq[2 * i + 1] = -1;
     }
     if (tid == 0) {
-        sh.qhead = sh.qtail = sh.rqhead = sh.rqtail = sh.idle = sh.ndone = 0;
-        sh.qcap = n;
-        sh.rqcap = 2 * n;
-        sh.exitkey = 0ull;
+        walk_reset(sh, 1, 2 * n);
+        sh.qcap[0] = n;
+        sh.graph = 0;
     }
     __syncthreads();
     /* earlier-neighbour masks and in-degrees */
@@ -1050,12 +1431,12 @@ __device__ void face_walk(const fd_station_dev &sd, Shared &sh, CtaSmem &cs, War
         }
         emask[i] = (unsigned char)em;
         dag[i] = (unsigned char)__popc(em);
-        if (em == 0) enqueue(queue, sh, i);
+        if (em == 0) enqueue_to(queue, sh.qtail[0], sh.qcap[0], sh, i);
     }
     __syncthreads();
     FD_TOC(0, t0);
     FD_TIC(tw);
-    run_walk(sd, sh, cs, ws, queue, n, dag, cn);
+    run_walk(sd, sh, cs, ws, n, dag, cn);
     __syncthreads();
     FD_TOC(4, tw);
     if (tid == 0) {
@@ -1101,79 +1482,171 @@ __device__ void setup_face(const fd_station_dev &sd, Shared &sh, int face)
     sh.n_pad = (sh.n + 15) & ~15;
 }
 
-/* One sweep of face F as a plane-pipelined dependency graph.  Leaves walls, flags and radius as
- * the radius loop of src/sphfd.c:1018-5566 would. */
-__device__ void pipelined_sweep(const fd_station_dev &sd, Shared &sh, CtaSmem &cs, WarpSmem &ws, Counters &cn, int F)
+/* One sweep (the radius loop of src/sphfd.c:1018-5566) as one dependency graph.  Leaves walls,
+ * flags, radius and the stencil-state carry as the radius loop would. */
+__device__ void graph_sweep(const fd_station_dev &sd, Shared &sh, CtaSmem &cs, WarpSmem &ws, Counters &cn)
 {
     const int tid = threadIdx.x;
-    const fdn_frame fr = frame_of(F);
-    if (tid == 0) {
-        setup_face(sd, sh, F);
-        /* the planes the radius loop would visit: up to grow[F] per radius step, until the wall
-         * reaches the model side or the radius reaches maxrad */
-        const int nmax = F < 2 ? sd.g.nz : F < 4 ? sd.g.nx : sd.g.ny;
-        int w = sh.wall[F], flag = sh.dflag[F], radius = sh.radius, rad0 = sh.rad0, np = 0;
-        while (rad0 && flag) {
-            for (int ig = 1; ig <= sd.grow[F]; ig++) {
-                if (!flag) continue;
-                np++;
-                if (fr.inner > 0 ? (w == 0) : (w == nmax - 1)) flag = 0;
-                w -= fr.inner;
-            }
-            radius++;
-            if (radius == sd.maxrad) rad0 = 0;
-        }
-        sh.np = np;
-        sh.player0 = sh.wall[F];
-        sh.wall[F] = w;
-        sh.dflag[F] = flag;
-        sh.radius = radius;
-        sh.rad0 = rad0;
-        sh.qhead = sh.qtail = sh.rqhead = sh.rqtail = sh.idle = sh.ndone = 0;
-        sh.qcap = (int)((long long)np * sh.n);
-        sh.rqcap = 0;
-        sh.exitkey = 0ull;
-        sh.pipelined = 1;
-    }
-    for (int k = tid; k < FDN_NTRIAL; k += blockDim.x) cs.desc[k] = c_desc[F * FDN_NTRIAL + k];
+    const int nx = sd.g.nx, ny = sd.g.ny, nz = sd.g.nz;
+    GraphSmem &gs = gsmem(sh);
+    FD_TIC(t0);
+    for (int k = tid; k < FDN_NFACE * FD_LMAX; k += blockDim.x) (&gs.lay2inst[0][0])[k] = -1;
     __syncthreads();
-    const int np = sh.np, nplane = sh.n, nuf = sh.nuf, nvf = nplane > 0 ? nplane / nuf : 0;
-    const long long total = (long long)np * nplane;
-    if (total > 0) {
-        for (long long id = tid; id < total; id += blockDim.x) sd.scr.pqueue[id] = -1;
-        __syncthreads();
-        /* counters: plane 0 reads the static wall layer, so its in-plane order is known now */
-        const int wall_layer = sh.player0 + fr.inner;
-        for (long long id = tid; id < total; id += blockDim.x) {
-            const int pp = (int)(id / nplane), i = (int)(id - (long long)pp * nplane);
-            const unsigned inr = inrect_mask(i % nuf, i / nuf, nuf, nvf);
-            const unsigned c2 = (unsigned)__popc(inr);
-            unsigned wd = (pp > 0 ? 1u + c2 : 0u) | (c2 << 8);
-            if (pp == 0) {
-                const unsigned em = earlier_mask(sd, sh, i, wall_layer);
-                sd.scr.pemask[id] = (unsigned char)em;
-                wd -= (unsigned)__popc(inr & ~em) << 8;
+    /* the sweep's face instances, as the radius loop visits them */
+    if (tid == 0) {
+        const int cap = sd.scr.ginst_cap < FD_IMAX ? sd.scr.ginst_cap : FD_IMAX;
+        int ninst = 0;
+        long long M = 0, per_face[6] = {0, 0, 0, 0, 0, 0};
+        unsigned faces = 0;
+        while (sh.rad0 && (sh.dflag[0] || sh.dflag[1] || sh.dflag[2] || sh.dflag[3] || sh.dflag[4] || sh.dflag[5])) {
+            for (int face = 0; face < 6; face++) {
+                for (int ig = 1; ig <= sd.grow[face]; ig++) {
+                    if (!sh.dflag[face]) continue;
+                    setup_face(sd, sh, face);
+                    if (sh.n > 0) {
+                        if (ninst >= cap) { sh.status = 13; break; }
+                        fd_ginst &gi = sd.scr.ginst[ninst];
+                        gi.face = face; gi.layer = sh.layer;
+                        gi.ulo = sh.ulo; gi.uhi = sh.uhi; gi.vlo = sh.vlo; gi.vhi = sh.vhi;
+                        gi.nuf = sh.nuf; gi.n = sh.n;
+                        gi.nkeyed = 0; gi.ndone = 0; gi.evwait = 0; gi.pad = 0; gi.exitkey = 0ull;
+                        GRect &gr = gs.rect[ninst];
+                        gr.face = (short)face; gr.layer = (short)sh.layer;
+                        gr.ulo = (short)sh.ulo; gr.uhi = (short)sh.uhi; gr.vlo = (short)sh.vlo; gr.vhi = (short)sh.vhi;
+                        gr.nuf = (short)sh.nuf; gr.pad = 0;
+                        gs.lay2inst[face][sh.layer] = (short)ninst;
+                        ninst++;
+                        M += sh.n;
+                        per_face[face] += sh.n;
+                        faces |= 1u << face;
+                    }
+                    /* move the wall outward (e.g. src/sphfd.c:1762-1764) */
+                    const int inner = frame_of(face).inner;
+                    const int nmax = face < 2 ? nz : face < 4 ? nx : ny;
+                    const bool limit = inner > 0 ? (sh.wall[face] == 0) : (sh.wall[face] == nmax - 1);
+                    if (limit) sh.dflag[face] = 0;
+                    sh.wall[face] -= inner;
+                }
             }
-            sd.scr.pcount[id] = wd;
-            if (wd == 0u) enqueue(sd.scr.pqueue, sh, (int)id);
+            sh.radius++;
+            if (sh.radius == sd.maxrad) sh.rad0 = 0;
+            if (sh.status) break;
         }
-        __syncthreads();
-        run_walk(sd, sh, cs, ws, sd.scr.pqueue, (int)total, nullptr, cn);
+        sh.ninst = ninst;
+        sh.gfaces = faces;
+        sh.single = __popc(faces) == 1;
+        sh.nodefer = 0;
+        sh.graph = 1;
+        walk_reset(sh, 6, FD_GRQ_CAP);
+        sh.nwait = 0;
+        long long b = 0;
+        for (int f = 0; f < 6; f++) { sh.qbase[f] = (int)b; sh.qcap[f] = (int)per_face[f]; b += per_face[f]; }
+        sh.gM = M;
+    }
+    __syncthreads();
+    const int ninst = sh.ninst;
+    const long long M = sh.gM;
+    if (sh.single) {
+        /* One face, every time below 1e9: every corner guard inside the grid passes, so each point
+         * calls a corner stencil before its 2-D trials and none needs an earlier point's state;
+         * the exception is the EAST corner whose guard tests the node above for being non-zero
+         * (src/sphfd.c:2544), which fails only next to a zero time. */
+        const int f = __ffs(sh.gfaces) - 1;
+        const long long nxyz = (long long)nx * ny * nz;
+        int bad = 0;
+        for (long long q = tid; q < nxyz; q += blockDim.x) {
+            const float t = sd.T[q];
+            if (!(t < 1.e9f)) bad = 1;
+            else if (f == 2 && t == 0.0f && (q / nx) % ny == 0 && q / ((long long)nx * ny) == 1) bad = 1;
+        }
+        bad = __syncthreads_or(bad);
+        if (tid == 0) sh.nodefer = !bad;
         __syncthreads();
     }
-    if (tid == 0) {
-        if (sh.exitkey) {
-            const float2 r = sd.scr.rec[(int)(sh.exitkey & 0xffffffffu)];
-            sh.carry_t0 = r.x;
-            sh.carry_t4 = r.y;
+    if (M > 0 && sh.status == 0) {
+        for (long long k = tid; k < M; k += blockDim.x) sd.scr.gqueue[k] = -1;
+        /* dependency counters */
+        for (int I = 0; I < ninst; I++) {
+            const GRect r = gs.rect[I];
+            const fdn_frame fr = frame_of(r.face);
+            const int n = rect_n(r), nvf = r.vhi - r.vlo + 1;
+            const unsigned myctx = sh.ctxm[r.face], myinn = sh.innm[r.face];
+            const bool prev = sh.single && I > 0 && gs.rect[I - 1].layer == r.layer + fr.inner;
+            for (int j = tid; j < n; j += blockDim.x) {
+                const long long p = inst_node(sd, r, j);
+                unsigned cin = 0, c2 = 0, cx = 0;
+                if (sh.single) {
+                    /* one face: the same-instance neighbours and the previous plane's inner block */
+                    const int iu = j % r.nuf, iv = j / r.nuf;
+                    c2 = (unsigned)__popc(inrect_mask(iu, iv, r.nuf, nvf));
+                    if (prev) {
+                        const GRect &rp = gs.rect[I - 1];
+                        const int u0 = r.ulo + iu, v0 = r.vlo + iv;
+                        for (int dv = -1; dv <= 1; dv++)
+                            for (int du = -1; du <= 1; du++)
+                                if (u0 + du >= rp.ulo && u0 + du <= rp.uhi && v0 + dv >= rp.vlo && v0 + dv <= rp.vhi) cin++;
+                    }
+                } else {
+                    const int pi = (int)p, pxy = pi / nx;
+                    const int x = pi - pxy * nx, y = pxy % ny, z = pxy / ny;
+                    for (int k = 0; k < 27; k++) {
+                        if (k == 13) continue;
+                        const int qx = x + k % 3 - 1, qy = y + (k / 3) % 3 - 1, qz = z + k / 9 - 1;
+                        if (qx < 0 || qx >= nx || qy < 0 || qy >= ny || qz < 0 || qz >= nz) continue;
+                        const int w = owner_of(gs, sh.gfaces, qx, qy, qz);
+                        if (w < 0 || own_inst(w) > I) continue;
+                        if (own_inst(w) == I) { c2++; continue; }
+                        if (!((myctx >> k) & 1u) && !((sh.ctxm[own_face(w)] >> (26 - k)) & 1u)) continue;
+                        if ((myinn >> k) & 1u) cin++; else cx++;
+                    }
+                }
+                sd.scr.gcnt[p] = cin | (c2 << 8) | (cx << 16);
+            }
         }
-        sh.faces += np;
-        sh.node_updates += total;
-        sh.psweeps++;
-        sh.pipelined = 0;
+        __syncthreads();
+        /* nodes whose inner block is final take their key now */
+        for (int I = 0; I < ninst; I++) {
+            const GRect r = gs.rect[I];
+            const int n = rect_n(r);
+            for (int j = tid; j < n; j += blockDim.x) {
+                const long long p = inst_node(sd, r, j);
+                if ((sd.scr.gcnt[p] & 0xFFu) == 0u && ready_word(key_event(sd, sh, I, j, p))) graph_ready(sd, sh, r.face, p);
+            }
+        }
+        __syncthreads();
+        FD_TOC(0, t0);
+        FD_TIC(tw);
+        run_walk(sd, sh, cs, ws, (int)M, nullptr, cn);
+        __syncthreads();
+        FD_TOC(4, tw);
+    }
+    /* the small tables back to their empty state for the next sweep */
+    {
+        const int nw = min(sh.nwait, FD_GWAIT_CAP), np = min(sh.npark, FD_GPARK_CAP), nr = min(sh.rqtail, FD_GRQ_CAP);
+        for (int k = tid; k < nw; k += blockDim.x) sd.scr.gwait[k] = make_int2(-1, -1);
+        for (int k = tid; k < np; k += blockDim.x) sd.scr.gpark[k] = make_int2(-1, -2);
+        for (int k = tid; k < nr; k += blockDim.x) sd.scr.grq[k] = -1;
+    }
+    if (tid == 0) {
+        /* the stencil state after the sweep: the record of its last writer */
+        for (int I = ninst - 1; I >= 0; I--) {
+            const unsigned long long ek = sd.scr.ginst[I].exitkey;
+            if (ek) {
+                const float2 r = sd.scr.grec[inst_node(sd, gs.rect[I], (int)(ek & 0xffffffffu))];
+                sh.carry_t0 = r.x;
+                sh.carry_t4 = r.y;
+                break;
+            }
+        }
+        sh.faces += ninst;
+        sh.node_updates += M;
+        sh.gsweeps++;
+        sh.graph = 0;
     }
     __syncthreads();
 }
+
+/* ---------------------------------------------------------------------------------------------- */
 
 /* source box (src/sphfd.c:724-825)                                                                */
 
@@ -1226,7 +1699,16 @@ __global__ void __launch_bounds__(FD_BLOCK, 1) fd_solve(const fd_station_dev *st
     if (tid == 0) asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t_start));
     /* the dependency bytes of the station's largest face go to shared memory when they fit */
     unsigned char *dag = 2ll * sd.max_face_pad <= dag_smem_bytes ? fd_dyn_smem + kSmemBase : sd.scr.dag;
+    const int gdim = sd.g.nx > sd.g.ny ? (sd.g.nx > sd.g.nz ? sd.g.nx : sd.g.nz) : (sd.g.ny > sd.g.nz ? sd.g.ny : sd.g.nz);
+    const bool gok = sd.scr.gcnt && gdim <= FD_LMAX && (int)sizeof(GraphSmem) <= dag_smem_bytes;
+    if (gok) {
+        /* the sweep-graph tables start empty */
+        for (int k = tid; k < FD_GWAIT_CAP; k += blockDim.x) sd.scr.gwait[k] = make_int2(-1, -1);
+        for (int k = tid; k < FD_GPARK_CAP; k += blockDim.x) sd.scr.gpark[k] = make_int2(-1, -2);
+        for (int k = tid; k < FD_GRQ_CAP; k += blockDim.x) sd.scr.grq[k] = -1;
+    }
     if (sd.init_mode == 0) init_field(sd);
+    for (int k = tid; k < FDN_NFACE * FDN_NTRIAL; k += blockDim.x) (&cs.desc[0][0])[k] = c_desc[k];
     if (tid == 0) {
         for (int f = 0; f < 6; f++) { sh.wall[f] = sd.wall[f]; sh.dflag[f] = sd.dflag[f]; }
         sh.radius = sd.radius;
@@ -1241,40 +1723,29 @@ __global__ void __launch_bounds__(FD_BLOCK, 1) fd_solve(const fd_station_dev *st
         sh.sweeps = 0;
         for (int k = 0; k < 8; k++) sh.restart_wall[k] = 0;
         for (int k = 0; k < 6; k++) sh.cyc[k] = 0;
-        sh.pipelined = 0;
-        sh.psweeps = 0;
+        sh.graph = 0;
+        sh.gsweeps = 0;
+        for (int f = 0; f < 6; f++) relation_masks(f, sh.ctxm[f], sh.innm[f]);
+        sh.gsm = fd_dyn_smem + kSmemBase;
+        sh.gok = gok;
+        sh.single = 0;
+        sh.nodefer = 0;
+        sh.gfaces = 0;
+        sh.nwait = 0;
+        sh.npark = 0;
     }
     __syncthreads();
     Counters cn;
     for (int k = 0; k < 5; k++) cn.n[k] = 0;
     const int nx = sd.g.nx, ny = sd.g.ny, nz = sd.g.nz;
-    const long long nxy = (long long)nx * ny;
     int guard_sweeps = 0;
     while (sh.reverse > -1 && sh.status == 0) {
         if (tid == 0) for (int k = 0; k < 8; k++) sh.headw[k] = 0;
         __syncthreads();
         FD_TIC(tsweep);
-        /* A sweep with one active face (every sweep after a restart) walks full planes.  It runs as
-         * one plane-pipelined graph when no point can need an earlier point's stencil state: every
-         * time below 1e9 makes every corner guard that is inside the grid pass (so each point calls
-         * a corner stencil before its 2-D trials), except the EAST corner whose guard tests the node
-         * above for being non-zero (src/sphfd.c:2544), which fails only next to a zero time. */
-        int act = -1, nact = 0;
-        for (int f = 0; f < 6; f++)
-            if (sh.dflag[f]) { act = f; nact++; }
-        bool piped = false;
-        if (nact == 1 && sh.rad0 && sd.scr.pcount) {
-            int bad = 0;
-            const long long nxyz = nxy * nz;
-            for (long long i = tid; i < nxyz; i += blockDim.x) {
-                const float t = sd.T[i];
-                if (!(t < 1.e9f)) bad = 1;
-                else if (act == 2 && t == 0.0f && (i / nx) % ny == 0 && i / nxy == 1) bad = 1;
-            }
-            piped = !__syncthreads_or(bad);
-        }
-        if (piped) pipelined_sweep(sd, sh, cs, ws, cn, act);
-        while (!piped && sh.rad0
+        const bool as_graph = sh.gok && (FD_GRAPH_FORWARD || sh.sweeps > 0);
+        if (as_graph) graph_sweep(sd, sh, cs, ws, cn);
+        while (!as_graph && sh.rad0
                && (sh.dflag[0] || sh.dflag[1] || sh.dflag[2] || sh.dflag[3] || sh.dflag[4] || sh.dflag[5])
                && sh.status == 0) {
             for (int face = 0; face < 6; face++) {
@@ -1348,7 +1819,7 @@ __global__ void __launch_bounds__(FD_BLOCK, 1) fd_solve(const fd_station_dev *st
         asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t_end));
         o->t_start_ns = (int64_t)t_start;
         o->t_end_ns = (int64_t)t_end;
-        o->pipelined_sweeps = (int32_t)sh.psweeps;
+        o->pipelined_sweeps = (int32_t)sh.gsweeps;
     }
 }
 
@@ -1372,8 +1843,9 @@ extern "C" cudaError_t fdk_launch_solve(const fd_station_dev *stations, int nst,
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     const long long base = (long long)fdk::kSmemBase;
-    const long long want = base + 2 * max_face_pad;
-    const long long bytes = want <= optin - 1024 ? want : base;
+    const long long graph = (long long)sizeof(fdk::GraphSmem);
+    const long long dagb = 2 * max_face_pad > graph ? 2 * max_face_pad : graph;
+    const long long bytes = base + dagb <= optin - 1024 ? base + dagb : (base + graph <= optin - 1024 ? base + graph : base);
     const cudaError_t e = cudaFuncSetAttribute(fdk::fd_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
     if (e != cudaSuccess) return e;
     fdk::fd_solve<<<nst, FD_BLOCK, (size_t)bytes, stream>>>(stations, nst, (int)(bytes - base));

@@ -75,6 +75,20 @@ typedef struct {
     int32_t pad;
 } fd_station_stats;
 
+/* One face instance of a sweep graph: a face walked at one wall position, with its point
+ * rectangle and its completion state. */
+typedef struct {
+    int face, layer, ulo, uhi, vlo, vhi, nuf, n;
+    int nkeyed, ndone;             /* points whose sort key is final; points done */
+    int evwait, pad;               /* bit 1: points wait for all keys, bit 2: for all points done */
+    unsigned long long exitkey;    /* largest key of a point that made a writer call (0: none) */
+} fd_ginst;
+
+/* sizes of the small sweep-graph tables */
+#define FD_GWAIT_CAP 65536   /* (awaited point, waiting point) pairs */
+#define FD_GPARK_CAP 65536   /* points parked on an instance event, and their wait states */
+#define FD_GRQ_CAP 262144    /* resume queue */
+
 /* Face-walk scratch of one station, sized for its largest face m (34 bytes per point):
  * key 8m | rec 8m | pst 4m | queue 4m | rq 8m | dag 2m (+32). */
 typedef struct {
@@ -85,12 +99,20 @@ typedef struct {
     int *rq;                   /* points waiting for an earlier point's (t0,t4), 2 entries per point */
     unsigned char *dag;        /* in-degree and earlier-neighbour bytes (2 per point) when they do
                                   not fit in shared memory */
-    /* plane-pipelined sweeps (NULL: not available, every face is walked on its own):
-     * one word per grid node (inner-layer dependencies pending in bits 0-7, in-plane ones in 8-15),
-     * the sweep's ready queue and each node's earlier-neighbour byte */
-    unsigned *pcount;
-    int *pqueue;
-    unsigned char *pemask;
+    /* sweep graphs (gcnt NULL: not available, every face is walked on its own).  Per grid node:
+     * dependency counter word (inner block pending in bits 0-7, same-instance neighbours in 8-15,
+     * other instances' nodes in 16-23, a point waits on it bit 29, done bit 30, sort key final
+     * bit 31), ready queue, earlier-neighbour byte, stencil-state record.  Small tables: the
+     * sweep's face instances, wait pairs, parked points, resume queue. */
+    unsigned *gcnt;
+    int *gqueue;
+    unsigned char *gemask;
+    float2 *grec;
+    fd_ginst *ginst;
+    int ginst_cap;
+    int2 *gwait;
+    int2 *gpark;
+    int *grq;
 } fd_scratch_dev;
 
 typedef struct {
