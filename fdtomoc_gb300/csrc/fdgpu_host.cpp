@@ -26,7 +26,7 @@
 extern "C" cudaError_t fdk_launch_geo_build(int nx, int ny, int nz, double h, double dq, double df, double z0r,
                                             const double *ysin, double *zrow, double *node, double *cell,
                                             cudaStream_t stream);
-extern "C" cudaError_t fdk_launch_solve(const fd_station_dev *stations, int nst, long long max_face_pad,
+extern "C" cudaError_t fdk_launch_solve(const fd_station_dev *stations, int nst, long long max_face_pad, int cluster,
                                         cudaStream_t stream);
 extern "C" cudaError_t fdk_launch_v2s(const float *v, float *s, long long n, cudaStream_t stream);
 extern "C" cudaError_t fdk_probe_fp64(double *scratch, int blocks, int threads, int iters, float *ms, cudaStream_t s);
@@ -77,6 +77,7 @@ uint64_t bits(double x)
 
 struct fdgpu_ctx {
     int device = 0;
+    int cluster = 0;   /* CTAs per station: 0 automatic */
     cudaStream_t stream = nullptr;
     std::map<GeoKey, std::unique_ptr<Geo>> geos;
     DevBuf scratch, stations, stats, trig, model, fields;
@@ -293,6 +294,14 @@ extern "C" int fdgpu_velocity_to_slowness(fdgpu_ctx *ctx, const float *v, float 
     return FDGPU_OK;
 }
 
+extern "C" int fdgpu_set_cluster(fdgpu_ctx *ctx, int ctas_per_station)
+{
+    if (!ctx || ctas_per_station < 0 || ctas_per_station > 8 || (ctas_per_station & (ctas_per_station - 1)))
+        return FDGPU_EINVAL;
+    ctx->cluster = ctas_per_station;
+    return FDGPU_OK;
+}
+
 extern "C" int fdgpu_solve_device(fdgpu_ctx *ctx, int n, const fdgpu_station *st, const float *slowness,
                                   long long s_sy, long long s_sz, float *const *d_times, int times_initialised,
                                   fdgpu_stats *stats, void *stream)
@@ -396,7 +405,7 @@ extern "C" int fdgpu_solve_device(fdgpu_ctx *ctx, int n, const fdgpu_station *st
     }
     FD_CU(ctx, cudaMemcpyAsync(ctx->trig.p, trig.data(), sizeof(double) * trig.size(), cudaMemcpyHostToDevice, cs));
     FD_CU(ctx, cudaMemcpyAsync(ctx->stations.p, hs.data(), sizeof(fd_station_dev) * n, cudaMemcpyHostToDevice, cs));
-    FD_CU(ctx, fdk_launch_solve(ctx->stations.as<fd_station_dev>(), n, max_pad, cs));
+    FD_CU(ctx, fdk_launch_solve(ctx->stations.as<fd_station_dev>(), n, max_pad, ctx->cluster, cs));
     std::vector<fd_station_stats> hst(n);
     FD_CU(ctx, cudaMemcpyAsync(hst.data(), ctx->stats.p, sizeof(fd_station_stats) * n, cudaMemcpyDeviceToHost, cs));
     FD_CU(ctx, cudaStreamSynchronize(cs));

@@ -24,6 +24,7 @@
  * counters (see "warp workers" below); every wait among them is bounded and ends in an error
  * status, never in a hang.
  */
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
@@ -121,26 +122,37 @@ __global__ void fd_geo_build(int nx, int ny, int nz, double h, double dq, double
 /* ---------------------------------------------------------------------------------------------- */
 /* per-CTA state                                                                                   */
 
-struct Shared {
-    int wall[6], dflag[6];
-    int radius, rad0, reverse, headpref;
-    int headw[8];
-    float carry_t0, carry_t4;
-    /* current walk: ready queues (one per face in a sweep graph; a face walk uses queue 0), the
-     * queue of points resuming a search for an inherited stencil state, idle workers, finished
-     * nodes, parked points */
+/* state of the current walk that all CTAs of a station's cluster share; it lives in the shared
+ * memory of the cluster's first CTA and the others reach it through distributed shared memory */
+struct WalkShared {
+    /* ready queues (one per face in a sweep graph; a face walk uses queue 0), the queue of points
+     * resuming a search for an inherited stencil state, idle workers, finished nodes, parked points
+     * and wait pairs */
     int nq;
     int qhead[6], qtail[6], qcap[6], qbase[6];
-    int rqhead, rqtail, rqcap, idle, ndone, npark;
+    int rqhead, rqtail, rqcap, idle, ndone, npark, nwait;
+    int status;
+    int headw[8];
     unsigned long long exitkey;
+    long long rounds, deferred;
+    unsigned long long st[5];
+    int bar_count, bar_gen;   /* cluster barrier: arrivals, generation */
+};
+
+struct Shared {
+    WalkShared wl;
+    WalkShared *w;           /* the cluster's shared walk state (wl of rank 0) */
+    int cs, rank;            /* CTAs per station, this CTA's rank */
+    int wall[6], dflag[6];
+    int radius, rad0, reverse, headpref;
+    float carry_t0, carry_t4;
     /* current face of a face walk */
     int face, layer, ulo, uhi, vlo, vhi, nuf, n, n_pad;
     long long su, sv, sn, ssu, ssv, ssn;
     int nu, nv;
-    int status;
     /* current sweep graph: on/off, face instances, points; per face, the 27-bit masks of the
      * neighbour offsets a node of that face reads, and of those in its inner plane */
-    int graph, gok, ninst, single, nodefer, nwait;
+    int graph, gok, ninst, single, nodefer;
     unsigned gfaces;
     long long gM;
     unsigned ctxm[6], innm[6];
@@ -148,13 +160,57 @@ struct Shared {
     unsigned long long red[FD_BLOCK / 32];
     unsigned long long bcast;
     /* statistics */
-    long long faces, node_updates, rounds, deferred;
-    unsigned long long st[5];
+    long long faces, node_updates;
     int sweeps;
     int restart_wall[8];
     long long cyc[6];
     long long gsweeps;
 };
+
+/* ordering of a worker's global and shared stores before the counters that publish them, at the
+ * scope of the CTAs that share the walk */
+__device__ __forceinline__ void wfence(const Shared &sh)
+{
+    if (sh.cs > 1)
+        asm volatile("fence.acq_rel.cluster;" ::: "memory");
+    else
+        __threadfence_block();
+}
+
+#ifndef FD_BAR_SPINS
+#define FD_BAR_SPINS (1ll << 26)   /* polls (about 64 ns apart) before a cluster barrier gives up */
+#endif
+
+/* Barrier of all threads of the station's CTAs: the CTA's threads meet, its thread 0 meets the other
+ * CTAs' at a generation counter in the first CTA's shared memory.  The wait is bounded: a CTA that
+ * waits too long records which barrier (site) gave up in the station's status and goes on, so a
+ * fault in the schedule ends in an error, never in a hang. */
+__device__ __forceinline__ void csync(Shared &sh, int site)
+{
+    __syncthreads();
+    if (sh.cs > 1) {
+        if (threadIdx.x == 0) {
+            asm volatile("fence.acq_rel.cluster;" ::: "memory");
+            const int gen = *const_cast<volatile int *>(&sh.w->bar_gen);
+            if (atomicAdd(&sh.w->bar_count, 1) == sh.cs - 1) {
+                sh.w->bar_count = 0;
+                asm volatile("fence.acq_rel.cluster;" ::: "memory");
+                atomicAdd(&sh.w->bar_gen, 1);
+            } else {
+                long long spins = 0;
+                while (*const_cast<volatile int *>(&sh.w->bar_gen) == gen) {
+                    __nanosleep(64);
+                    if (++spins > FD_BAR_SPINS) {
+                        atomicCAS(&sh.w->status, 0, 100 + site);
+                        break;
+                    }
+                }
+            }
+            asm volatile("fence.acq_rel.cluster;" ::: "memory");
+        }
+        __syncthreads();
+    }
+}
 
 /* face frame for a face number known only at run time */
 __device__ __forceinline__ fdn_frame frame_of(int f)
@@ -235,6 +291,9 @@ struct Counters {
 
 #define NB_PAD 19                    /* context row stride: the 32 rows fall on distinct banks */
 #define FD_WAIT_CYCLES (4ll << 30)   /* about 2 s at the maximum SM clock */
+#ifndef FD_WALK_CYCLES
+#define FD_WALK_CYCLES (1ll << 37)   /* about 66 s: no walk of a real grid comes near it */
+#endif
 #define FD_QSPIN (1 << 22)           /* polls of an unwritten queue entry before giving up */
 #define FD_KEYED 0x80000000u         /* counter word: the node's sort key is final */
 
@@ -550,9 +609,9 @@ __device__ __forceinline__ void enqueue_to(int *queue, int &tail, int cap, Share
 {
     const int pos = atomicAdd(&tail, 1);
     if (pos < cap)
-        queue[pos] = e;
+        *const_cast<volatile int *>(&queue[pos]) = e;   /* a strong store: readers synchronise on it */
     else
-        atomicCAS(&sh.status, 0, 10);
+        atomicCAS(&sh.w->status, 0, 10);
 }
 
 /* ---------------------------------------------------------------------------------------------- */
@@ -564,14 +623,14 @@ __device__ void face_release(const fd_station_dev &sd, Shared &sh, unsigned char
 {
     if (writer) {
         sd.scr.rec[i] = make_float2(st0, st4);
-        atomicMax(&sh.exitkey, sd.scr.key[i]);
+        atomicMax(&sh.w->exitkey, sd.scr.key[i]);
     } else {
         sd.scr.rec[i] = make_float2(__int_as_float(0x7fc00000), __int_as_float(0x7fc00000));
     }
-    __threadfence_block();
+    wfence(sh);
     /* done; a point waiting for the stencil state left before it resumes its search */
     const int waiter = atomicExch(&sd.scr.pst[i], -2);
-    if (waiter >= 0) enqueue_to(sd.scr.rq, sh.rqtail, sh.rqcap, sh, waiter);
+    if (waiter >= 0) enqueue_to(sd.scr.rq, sh.w->rqtail, sh.w->rqcap, sh, waiter);
     const int nvf = sh.n / sh.nuf, iu = i % sh.nuf, iv = i / sh.nuf;
     const unsigned char *emask = dag + sh.n_pad;
     unsigned later = inrect_mask(iu, iv, sh.nuf, nvf) & ~(unsigned)emask[i];
@@ -584,7 +643,7 @@ __device__ void face_release(const fd_station_dev &sd, Shared &sh, unsigned char
         const int j = (iv + dv) * sh.nuf + iu + du;
         const unsigned sh8 = (j & 3) * 8;
         const unsigned old = atomicSub(reinterpret_cast<unsigned *>(dag) + (j >> 2), 1u << sh8);
-        if (((old >> sh8) & 0xFFu) == 1u) enqueue_to(sd.scr.queue, sh.qtail[0], sh.qcap[0], sh, j);
+        if (((old >> sh8) & 0xFFu) == 1u) enqueue_to(sd.scr.queue, sh.w->qtail[0], sh.w->qcap[0], sh, j);
     }
 }
 
@@ -710,14 +769,14 @@ __device__ __forceinline__ int inst_fill(const GRect &r, const int xyz[3])
 /* points parked on instance I's event `kind` (1: all keys final, 2: all done) go to the resume queue */
 __device__ void fire_event(const fd_station_dev &sd, Shared &sh, int I, int kind)
 {
-    __threadfence_block();
+    wfence(sh);
     if (!(vload(sd.scr.ginst[I].evwait) & kind)) return;
     const int st = (kind << 24) | I;
-    const int np = min(vload(sh.npark), FD_GPARK_CAP);
+    const int np = min(vload(sh.w->npark), FD_GPARK_CAP);
     for (int k = 0; k < np; k++) {
         if (vload(sd.scr.gpark[k].y) == st && atomicCAS(&sd.scr.gpark[k].y, st, -2) == st) {
-            __threadfence_block();
-            enqueue_to(sd.scr.grq, sh.rqtail, sh.rqcap, sh, vload(sd.scr.gpark[k].x));
+            wfence(sh);
+            enqueue_to(sd.scr.grq, sh.w->rqtail, sh.w->rqcap, sh, vload(sd.scr.gpark[k].x));
         }
     }
 }
@@ -750,7 +809,7 @@ __device__ unsigned key_event(const fd_station_dev &sd, Shared &sh, int I, int j
         if (((inr >> k) & 1u) && node_key(tn[k], j + du + dv * r.nuf) < kj) em |= 1u << k;
     }
     sd.scr.gemask[q] = (unsigned char)em;
-    __threadfence_block();
+    wfence(sh);
     const unsigned lat = (unsigned)__popc(inr & ~em);
     const unsigned add = FD_KEYED - (lat << 8);
     const unsigned nw = atomicAdd(&sd.scr.gcnt[q], add) + add;
@@ -762,7 +821,7 @@ __device__ __forceinline__ bool ready_word(unsigned w) { return (w & ~FD_WAITB) 
 
 __device__ __forceinline__ void graph_ready(const fd_station_dev &sd, Shared &sh, int face, long long q)
 {
-    enqueue_to(sd.scr.gqueue + sh.qbase[face], sh.qtail[face], sh.qcap[face], sh, (int)q);
+    enqueue_to(sd.scr.gqueue + sh.w->qbase[face], sh.w->qtail[face], sh.w->qcap[face], sh, (int)q);
 }
 
 /* drop one inner-block (inner) or other-instance dependency of node q (instance oq, face fq) */
@@ -796,14 +855,14 @@ __device__ void graph_release(const fd_station_dev &sd, Shared &sh, int F, long 
             sd.scr.grec[p] = make_float2(__int_as_float(0x7fc00000), __int_as_float(0x7fc00000));
         }
     }
-    __threadfence_block();
+    wfence(sh);
     /* done; a point waiting for the stencil state left before it resumes its search */
     if (!sh.nodefer && (atomicOr(&sd.scr.gcnt[p], FD_DONEB) & FD_WAITB)) {
-        __threadfence_block();
-        const int nw = min(vload(sh.nwait), FD_GWAIT_CAP);
+        wfence(sh);
+        const int nw = min(vload(sh.w->nwait), FD_GWAIT_CAP);
         for (int k = 0; k < nw; k++)
             if (vload(sd.scr.gwait[k].x) == (int)p && atomicCAS(&sd.scr.gwait[k].x, (int)p, -1) == (int)p)
-                enqueue_to(sd.scr.grq, sh.rqtail, sh.rqcap, sh, vload(sd.scr.gwait[k].y));
+                enqueue_to(sd.scr.grq, sh.w->rqtail, sh.w->rqcap, sh, vload(sd.scr.gwait[k].y));
     }
     const int nx = sd.g.nx, ny = sd.g.ny;
     const int x = pxyz[0], y = pxyz[1], z = pxyz[2];
@@ -845,7 +904,7 @@ __device__ void graph_release(const fd_station_dev &sd, Shared &sh, int F, long 
     }
     /* later neighbours in the same instance */
     const int nvf = r.vhi - r.vlo + 1, iu = i % r.nuf, iv = i / r.nuf;
-    unsigned later = inrect_mask(iu, iv, r.nuf, nvf) & ~(unsigned)sd.scr.gemask[p];
+    unsigned later = inrect_mask(iu, iv, r.nuf, nvf) & ~(unsigned)__ldcg(&sd.scr.gemask[p]);
     while (later) {
         const int k = __ffs(later) - 1;
         later &= later - 1;
@@ -860,34 +919,34 @@ __device__ void graph_release(const fd_station_dev &sd, Shared &sh, int F, long 
 /* point w waits for an event of instance I (kind 1: all keys final, 2: all points done) (lane 0) */
 __device__ void wait_event(const fd_station_dev &sd, Shared &sh, int w, int I, int kind)
 {
-    const int k = atomicAdd(&sh.npark, 1);
+    const int k = atomicAdd(&sh.w->npark, 1);
     if (k >= FD_GPARK_CAP) {
-        atomicCAS(&sh.status, 0, 15);
+        atomicCAS(&sh.w->status, 0, 15);
         return;
     }
     const int st = (kind << 24) | I;
     sd.scr.gpark[k].x = w;
-    __threadfence_block();
+    wfence(sh);
     atomicExch(&sd.scr.gpark[k].y, st);
     atomicOr(&sd.scr.ginst[I].evwait, kind);
-    __threadfence_block();
+    wfence(sh);
     const int n = rect_n(gsmem(sh).rect[I]);
     const bool now = kind == 1 ? vload(sd.scr.ginst[I].nkeyed) >= n : vload(sd.scr.ginst[I].ndone) >= n;
-    if (now && atomicCAS(&sd.scr.gpark[k].y, st, -2) == st) enqueue_to(sd.scr.grq, sh.rqtail, sh.rqcap, sh, w);
+    if (now && atomicCAS(&sd.scr.gpark[k].y, st, -2) == st) enqueue_to(sd.scr.grq, sh.w->rqtail, sh.w->rqcap, sh, w);
 }
 
 /* point w waits for point p to be done (lane 0).  Returns false if p is already done (no wait). */
 __device__ bool wait_point(const fd_station_dev &sd, Shared &sh, int w, long long p)
 {
-    const int k = atomicAdd(&sh.nwait, 1);
+    const int k = atomicAdd(&sh.w->nwait, 1);
     if (k >= FD_GWAIT_CAP) {
-        atomicCAS(&sh.status, 0, 15);
+        atomicCAS(&sh.w->status, 0, 15);
         return true;
     }
     sd.scr.gwait[k].y = w;
-    __threadfence_block();
+    wfence(sh);
     atomicExch(&sd.scr.gwait[k].x, (int)p);
-    __threadfence_block();
+    wfence(sh);
     if (!(atomicOr(&sd.scr.gcnt[p], FD_WAITB) & FD_DONEB)) return true;
     /* p finished meanwhile: take the pair back unless p's release already took it (and queued w) */
     return atomicCAS(&sd.scr.gwait[k].x, (int)p, -1) != (int)p;
@@ -961,7 +1020,7 @@ __device__ bool commit_node(const fd_station_dev &sd, Shared &sh, const TrialDes
         if (lastK >= 0) {
             /* only the last head trial that lowered the minimum sets the measure that is tested */
             const double fhead = (last_gb - last_v) / head_den(dsc[lastK], s18, sd.g, z, y);
-            if (fhead > FD_HEADTEST) atomicAdd(&sh.headw[frame_of(F).headw], 1);
+            if (fhead > FD_HEADTEST) atomicAdd(&sh.w->headw[frame_of(F).headw], 1);
         }
     }
     if (sh.graph)
@@ -1027,7 +1086,7 @@ __device__ void warp_chunk(const fd_station_dev &sd, Shared &sh, const CtaSmem &
         bool ok;
         wh = locate(sd, sh, F, e, ok);
         if (!ok) {
-            atomicCAS(&sh.status, 0, 14);   /* a queued node no face instance owns */
+            atomicCAS(&sh.w->status, 0, 14);   /* a queued node no face instance owns */
             e = -1;
         }
     }
@@ -1046,7 +1105,8 @@ __device__ void warp_chunk(const fd_station_dev &sd, Shared &sh, const CtaSmem &
             const int uu = wh.r.u + du, vv = wh.r.v + dv;
             float tv = 0.f, svv = 0.f;
             if (uu >= 0 && uu < wh.r.nu && vv >= 0 && vv < wh.r.nv) {
-                tv = sd.T[wh.p + du * su + dv * sv + (w ? inner_t : 0ll)];
+                /* through L2: another SM may have written it since this SM last read it */
+                tv = __ldcg(&sd.T[wh.p + du * su + dv * sv + (w ? inner_t : 0ll)]);
                 svv = __ldg(&sd.S[pS + du * ssu + dv * ssv + (w ? inner_s : 0ll)]);
             }
             tr[nb] = tv;
@@ -1081,11 +1141,11 @@ __device__ void warp_chunk(const fd_station_dev &sd, Shared &sh, const CtaSmem &
     if (valid) {
         fin = commit_node(sd, sh, dsc, ws, lane, F, wh, gm, em, p0, p4, permissive, dag, cn);
         if (!fin) {
-            atomicAdd(reinterpret_cast<unsigned long long *>(&sh.deferred), 1ull);
+            atomicAdd(reinterpret_cast<unsigned long long *>(&sh.w->deferred), 1ull);
             if (sh.nodefer)
-                atomicCAS(&sh.status, 0, 6);   /* excluded by the sweep's precondition */
+                atomicCAS(&sh.w->status, 0, 6);   /* excluded by the sweep's precondition */
             else
-                enqueue_to(sh.graph ? sd.scr.grq : sd.scr.rq, sh.rqtail, sh.rqcap, sh, e);
+                enqueue_to(sh.graph ? sd.scr.grq : sd.scr.rq, sh.w->rqtail, sh.w->rqcap, sh, e);
         }
     }
     if (sh.graph && !sh.nodefer) {
@@ -1101,8 +1161,8 @@ __device__ void warp_chunk(const fd_station_dev &sd, Shared &sh, const CtaSmem &
     }
     const unsigned done = __ballot_sync(0xffffffffu, fin);
     if (lane == 0 && done) {
-        __threadfence_block();
-        atomicAdd(&sh.ndone, __popc(done));
+        wfence(sh);
+        atomicAdd(&sh.w->ndone, __popc(done));
     }
     __syncwarp();
     FD_TOC(3, tc);
@@ -1156,10 +1216,10 @@ __device__ void resume_waiter(const fd_station_dev &sd, Shared &sh, const CtaSme
                     const int old = atomicCAS(&sd.scr.pst[p], -1, w);
                     if (old == -1) verdict = 2;
                     else if (old == -2) verdict = 3;
-                    else { atomicCAS(&sh.status, 0, 11); verdict = 2; }   /* a second waiter */
+                    else { atomicCAS(&sh.w->status, 0, 11); verdict = 2; }   /* a second waiter */
                 }
                 if (verdict == 0 || verdict == 3) {
-                    __threadfence_block();
+                    wfence(sh);
                     const float r0 = vload(sd.scr.rec[p].x), r4 = vload(sd.scr.rec[p].y);
                     if (!isnan(r0)) { verdict = 1; t0 = r0; t4 = r4; }
                     else verdict = 0;
@@ -1176,7 +1236,7 @@ __device__ void resume_waiter(const fd_station_dev &sd, Shared &sh, const CtaSme
         }
         c = p;
     }
-    if (lane == 0) atomicCAS(&sh.status, 0, 12);
+    if (lane == 0) atomicCAS(&sh.w->status, 0, 12);
 }
 
 /* Sweep graph: the same search for point w (a grid index), by the reference's order of face
@@ -1192,7 +1252,7 @@ __device__ void resume_graph(const fd_station_dev &sd, Shared &sh, const CtaSmem
     const int xyz[3] = {w - wxy * nx, wxy % ny, wxy / ny};
     const int ow = owner_of(gs, sh.gfaces, xyz[0], xyz[1], xyz[2]);
     if (ow < 0) {
-        if (lane == 0) atomicCAS(&sh.status, 0, 14);
+        if (lane == 0) atomicCAS(&sh.w->status, 0, 14);
         return;
     }
     const int I = own_inst(ow);
@@ -1219,7 +1279,7 @@ __device__ void resume_graph(const fd_station_dev &sd, Shared &sh, const CtaSmem
                 if (!(vload(sd.scr.gcnt[p]) & FD_DONEB) && wait_point(sd, sh, w, p)) {
                     verdict = 2;
                 } else {
-                    __threadfence_block();
+                    wfence(sh);
                     const float r0 = vload(sd.scr.grec[p].x), r4 = vload(sd.scr.grec[p].y);
                     if (!isnan(r0)) { verdict = 1; t0 = r0; t4 = r4; }
                 }
@@ -1229,7 +1289,7 @@ __device__ void resume_graph(const fd_station_dev &sd, Shared &sh, const CtaSmem
                 for (int J = I - 1; J >= 0; J--) {
                     const GRect &rj = gs.rect[J];
                     if (vload(sd.scr.ginst[J].ndone) < rect_n(rj)) { wait_event(sd, sh, w, J, 2); verdict = 2; break; }
-                    __threadfence_block();
+                    wfence(sh);
                     const unsigned long long ek = vload(sd.scr.ginst[J].exitkey);
                     if (ek) {
                         const long long p = inst_node(sd, rj, (int)(ek & 0xffffffffu));
@@ -1250,7 +1310,7 @@ __device__ void resume_graph(const fd_station_dev &sd, Shared &sh, const CtaSmem
         }
         kc = best;
     }
-    if (lane == 0) atomicCAS(&sh.status, 0, 12);
+    if (lane == 0) atomicCAS(&sh.w->status, 0, 12);
 }
 
 /* ---------------------------------------------------------------------------------------------- */
@@ -1259,18 +1319,18 @@ __device__ void resume_graph(const fd_station_dev &sd, Shared &sh, const CtaSmem
 /* nothing queued, every worker idle, and all queues unchanged across the idle count (lane 0) */
 __device__ __forceinline__ bool quiescent(Shared &sh)
 {
-    int t0[6], r0 = vload(sh.rqtail);
-    for (int k = 0; k < sh.nq; k++) {
-        t0[k] = vload(sh.qtail[k]);
-        if (vload(sh.qhead[k]) != t0[k]) return false;
+    int t0[6], r0 = vload(sh.w->rqtail);
+    for (int k = 0; k < sh.w->nq; k++) {
+        t0[k] = vload(sh.w->qtail[k]);
+        if (vload(sh.w->qhead[k]) != t0[k]) return false;
     }
-    if (vload(sh.rqhead) != r0) return false;
-    __threadfence_block();
-    if (vload(sh.idle) != FD_WARPS) return false;
-    __threadfence_block();
-    for (int k = 0; k < sh.nq; k++)
-        if (vload(sh.qtail[k]) != t0[k] || vload(sh.qhead[k]) != t0[k]) return false;
-    return vload(sh.rqtail) == r0 && vload(sh.rqhead) == r0;
+    if (vload(sh.w->rqhead) != r0) return false;
+    wfence(sh);
+    if (vload(sh.w->idle) != sh.cs * FD_WARPS) return false;
+    wfence(sh);
+    for (int k = 0; k < sh.w->nq; k++)
+        if (vload(sh.w->qtail[k]) != t0[k] || vload(sh.w->qhead[k]) != t0[k]) return false;
+    return vload(sh.w->rqtail) == r0 && vload(sh.w->rqhead) == r0;
 }
 
 /* read a claimed queue entry: spins briefly for an entry whose writer is between its two
@@ -1283,7 +1343,7 @@ __device__ __forceinline__ int read_entry(const int *queue, int pos, Shared &sh)
         __nanosleep(32);
         e = *q;
     }
-    if (e < 0) atomicCAS(&sh.status, 0, 9);   /* a claimed entry never written */
+    if (e < 0) atomicCAS(&sh.w->status, 0, 9);   /* a claimed entry never written */
     return e;
 }
 
@@ -1297,37 +1357,38 @@ __device__ void run_walk(const fd_station_dev &sd, Shared &sh, const CtaSmem &cs
     int *rq = sh.graph ? sd.scr.grq : sd.scr.rq;
     bool idle = false;
     long long since = clock64();
+    const long long started = since;
     long long chunks = 0;
     for (;;) {
         int act = 0, h = 0, m = 0, qf = 0;   /* act: 0 wait, 1 chunk, 2 resume a waiter, 3 leave */
         if (lane == 0) {
-            if (vload(sh.status) != 0 || vload(sh.ndone) >= total) {
+            if (vload(sh.w->status) != 0 || vload(sh.w->ndone) >= total) {
                 act = 3;
             } else {
-                const int rh = vload(sh.rqhead), rt0 = vload(sh.rqtail), rt = rt0 < sh.rqcap ? rt0 : sh.rqcap;
+                const int rh = vload(sh.w->rqhead), rt0 = vload(sh.w->rqtail), rt = rt0 < sh.w->rqcap ? rt0 : sh.w->rqcap;
                 if (rh < rt) {
-                    if (idle) { atomicSub(&sh.idle, 1); idle = false; }
-                    if (atomicCAS(&sh.rqhead, rh, rh + 1) == rh) { act = 2; h = read_entry(rq, rh, sh); }
+                    if (idle) { atomicSub(&sh.w->idle, 1); idle = false; }
+                    if (atomicCAS(&sh.w->rqhead, rh, rh + 1) == rh) { act = 2; h = read_entry(rq, rh, sh); }
                 } else {
                     /* the fullest queue, starting the scan at a warp-dependent face */
                     int best = -1, bavail = 0, bhead = 0;
-                    for (int k0 = 0; k0 < sh.nq; k0++) {
-                        const int k = (k0 + warp) % sh.nq;
-                        const int hd = vload(sh.qhead[k]), qt = vload(sh.qtail[k]);
-                        const int tl = qt < sh.qcap[k] ? qt : sh.qcap[k];
+                    for (int k0 = 0; k0 < sh.w->nq; k0++) {
+                        const int k = (k0 + warp) % sh.w->nq;
+                        const int hd = vload(sh.w->qhead[k]), qt = vload(sh.w->qtail[k]);
+                        const int tl = qt < sh.w->qcap[k] ? qt : sh.w->qcap[k];
                         if (tl - hd > bavail) { bavail = tl - hd; best = k; bhead = hd; }
                     }
                     if (best >= 0) {
-                        if (idle) { atomicSub(&sh.idle, 1); idle = false; }
+                        if (idle) { atomicSub(&sh.w->idle, 1); idle = false; }
                         const int want = bavail < 32 ? bavail : 32;
-                        if (atomicCAS(&sh.qhead[best], bhead, bhead + want) == bhead) {
-                            act = 1; h = sh.qbase[best] + bhead; m = want; qf = best;
+                        if (atomicCAS(&sh.w->qhead[best], bhead, bhead + want) == bhead) {
+                            act = 1; h = sh.w->qbase[best] + bhead; m = want; qf = best;
                         }
                     } else {
-                        if (!idle) { __threadfence_block(); atomicAdd(&sh.idle, 1); idle = true; }
+                        if (!idle) { wfence(sh); atomicAdd(&sh.w->idle, 1); idle = true; }
                         /* all idle with nothing queued and nodes left: nothing can release them */
-                        if (quiescent(sh) && vload(sh.ndone) < total) {
-                            atomicCAS(&sh.status, 0, 3);
+                        if (quiescent(sh) && vload(sh.w->ndone) < total) {
+                            atomicCAS(&sh.w->status, 0, 3);
                             act = 3;
                         }
                     }
@@ -1335,7 +1396,11 @@ __device__ void run_walk(const fd_station_dev &sd, Shared &sh, const CtaSmem &cs
                 if (act == 1 || act == 2) {
                     since = clock64();
                 } else if (act == 0 && clock64() - since > FD_WAIT_CYCLES) {
-                    atomicCAS(&sh.status, 0, 8);   /* no work for this worker for too long */
+                    atomicCAS(&sh.w->status, 0, 8);   /* no work for this worker for too long */
+                    act = 3;
+                }
+                if (act != 3 && clock64() - started > FD_WALK_CYCLES) {
+                    atomicCAS(&sh.w->status, 0, 17);   /* the walk as a whole ran far too long */
                     act = 3;
                 }
             }
@@ -1354,15 +1419,15 @@ __device__ void run_walk(const fd_station_dev &sd, Shared &sh, const CtaSmem &cs
                     __nanosleep(32);
                     e = *q;
                 }
-                if (e < 0) atomicCAS(&sh.status, 0, 9);   /* a claimed entry never written */
+                if (e < 0) atomicCAS(&sh.w->status, 0, 9);   /* a claimed entry never written */
             }
-            __threadfence_block();
+            wfence(sh);
             warp_chunk(sd, sh, cs, ws, sh.graph ? qf : sh.face, e, false, 0.f, 0.f, dag, cn);
             chunks++;
             continue;
         }
         if (act == 2) {
-            __threadfence_block();
+            wfence(sh);
             if (h >= 0) {
                 if (sh.graph)
                     resume_graph(sd, sh, cs, ws, h, cn);
@@ -1373,17 +1438,17 @@ __device__ void run_walk(const fd_station_dev &sd, Shared &sh, const CtaSmem &cs
         }
         __nanosleep(64);
     }
-    if (lane == 0 && chunks) atomicAdd(reinterpret_cast<unsigned long long *>(&sh.rounds), (unsigned long long)chunks);
+    if (lane == 0 && chunks) atomicAdd(reinterpret_cast<unsigned long long *>(&sh.w->rounds), (unsigned long long)chunks);
 }
 
 /* reset the walk counters (thread 0) */
 __device__ void walk_reset(Shared &sh, int nq, int rqcap)
 {
-    sh.nq = nq;
-    for (int k = 0; k < 6; k++) { sh.qhead[k] = 0; sh.qtail[k] = 0; sh.qcap[k] = 0; sh.qbase[k] = 0; }
-    sh.rqhead = sh.rqtail = sh.idle = sh.ndone = sh.npark = 0;
-    sh.rqcap = rqcap;
-    sh.exitkey = 0ull;
+    sh.w->nq = nq;
+    for (int k = 0; k < 6; k++) { sh.w->qhead[k] = 0; sh.w->qtail[k] = 0; sh.w->qcap[k] = 0; sh.w->qbase[k] = 0; }
+    sh.w->rqhead = sh.w->rqtail = sh.w->idle = sh.w->ndone = sh.w->npark = 0;
+    sh.w->rqcap = rqcap;
+    sh.w->exitkey = 0ull;
 }
 
 /* Walk the current face (parameters in sh) in dependency order. */
@@ -1412,7 +1477,7 @@ __device__ void face_walk(const fd_station_dev &sd, Shared &sh, CtaSmem &cs, War
     }
     if (tid == 0) {
         walk_reset(sh, 1, 2 * n);
-        sh.qcap[0] = n;
+        sh.w->qcap[0] = n;
         sh.graph = 0;
     }
     __syncthreads();
@@ -1431,7 +1496,7 @@ __device__ void face_walk(const fd_station_dev &sd, Shared &sh, CtaSmem &cs, War
         }
         emask[i] = (unsigned char)em;
         dag[i] = (unsigned char)__popc(em);
-        if (em == 0) enqueue_to(queue, sh.qtail[0], sh.qcap[0], sh, i);
+        if (em == 0) enqueue_to(queue, sh.w->qtail[0], sh.w->qcap[0], sh, i);
     }
     __syncthreads();
     FD_TOC(0, t0);
@@ -1440,8 +1505,8 @@ __device__ void face_walk(const fd_station_dev &sd, Shared &sh, CtaSmem &cs, War
     __syncthreads();
     FD_TOC(4, tw);
     if (tid == 0) {
-        if (sh.exitkey) {
-            const float2 r = sd.scr.rec[(int)(sh.exitkey & 0xffffffffu)];
+        if (sh.w->exitkey) {
+            const float2 r = sd.scr.rec[(int)(sh.w->exitkey & 0xffffffffu)];
             sh.carry_t0 = r.x;
             sh.carry_t4 = r.y;
         }
@@ -1487,6 +1552,9 @@ __device__ void setup_face(const fd_station_dev &sd, Shared &sh, int face)
 __device__ void graph_sweep(const fd_station_dev &sd, Shared &sh, CtaSmem &cs, WarpSmem &ws, Counters &cn)
 {
     const int tid = threadIdx.x;
+    /* the station's threads over all its CTAs, for loops over nodes */
+    const int gt = sh.rank * blockDim.x + tid, gstride = sh.cs * blockDim.x;
+    const bool lead = sh.rank == 0;
     const int nx = sd.g.nx, ny = sd.g.ny, nz = sd.g.nz;
     GraphSmem &gs = gsmem(sh);
     FD_TIC(t0);
@@ -1498,18 +1566,21 @@ __device__ void graph_sweep(const fd_station_dev &sd, Shared &sh, CtaSmem &cs, W
         int ninst = 0;
         long long M = 0, per_face[6] = {0, 0, 0, 0, 0, 0};
         unsigned faces = 0;
+        bool over = false;
         while (sh.rad0 && (sh.dflag[0] || sh.dflag[1] || sh.dflag[2] || sh.dflag[3] || sh.dflag[4] || sh.dflag[5])) {
             for (int face = 0; face < 6; face++) {
                 for (int ig = 1; ig <= sd.grow[face]; ig++) {
                     if (!sh.dflag[face]) continue;
                     setup_face(sd, sh, face);
                     if (sh.n > 0) {
-                        if (ninst >= cap) { sh.status = 13; break; }
-                        fd_ginst &gi = sd.scr.ginst[ninst];
-                        gi.face = face; gi.layer = sh.layer;
-                        gi.ulo = sh.ulo; gi.uhi = sh.uhi; gi.vlo = sh.vlo; gi.vhi = sh.vhi;
-                        gi.nuf = sh.nuf; gi.n = sh.n;
-                        gi.nkeyed = 0; gi.ndone = 0; gi.evwait = 0; gi.pad = 0; gi.exitkey = 0ull;
+                        if (ninst >= cap) { over = true; break; }
+                        if (lead) {
+                            fd_ginst &gi = sd.scr.ginst[ninst];
+                            gi.face = face; gi.layer = sh.layer;
+                            gi.ulo = sh.ulo; gi.uhi = sh.uhi; gi.vlo = sh.vlo; gi.vhi = sh.vhi;
+                            gi.nuf = sh.nuf; gi.n = sh.n;
+                            gi.nkeyed = 0; gi.ndone = 0; gi.evwait = 0; gi.pad = 0; gi.exitkey = 0ull;
+                        }
                         GRect &gr = gs.rect[ninst];
                         gr.face = (short)face; gr.layer = (short)sh.layer;
                         gr.ulo = (short)sh.ulo; gr.uhi = (short)sh.uhi; gr.vlo = (short)sh.vlo; gr.vhi = (short)sh.vhi;
@@ -1530,20 +1601,23 @@ __device__ void graph_sweep(const fd_station_dev &sd, Shared &sh, CtaSmem &cs, W
             }
             sh.radius++;
             if (sh.radius == sd.maxrad) sh.rad0 = 0;
-            if (sh.status) break;
+            if (over) break;
         }
         sh.ninst = ninst;
         sh.gfaces = faces;
         sh.single = __popc(faces) == 1;
         sh.nodefer = 0;
         sh.graph = 1;
-        walk_reset(sh, 6, FD_GRQ_CAP);
-        sh.nwait = 0;
-        long long b = 0;
-        for (int f = 0; f < 6; f++) { sh.qbase[f] = (int)b; sh.qcap[f] = (int)per_face[f]; b += per_face[f]; }
         sh.gM = M;
+        if (lead) {
+            if (over) sh.w->status = 13;
+            walk_reset(sh, 6, FD_GRQ_CAP);
+            sh.w->nwait = 0;
+            long long b = 0;
+            for (int f = 0; f < 6; f++) { sh.w->qbase[f] = (int)b; sh.w->qcap[f] = (int)per_face[f]; b += per_face[f]; }
+        }
     }
-    __syncthreads();
+    csync(sh, 1);
     const int ninst = sh.ninst;
     const long long M = sh.gM;
     if (sh.single) {
@@ -1555,7 +1629,7 @@ __device__ void graph_sweep(const fd_station_dev &sd, Shared &sh, CtaSmem &cs, W
         const long long nxyz = (long long)nx * ny * nz;
         int bad = 0;
         for (long long q = tid; q < nxyz; q += blockDim.x) {
-            const float t = sd.T[q];
+            const float t = __ldcg(&sd.T[q]);
             if (!(t < 1.e9f)) bad = 1;
             else if (f == 2 && t == 0.0f && (q / nx) % ny == 0 && q / ((long long)nx * ny) == 1) bad = 1;
         }
@@ -1563,8 +1637,8 @@ __device__ void graph_sweep(const fd_station_dev &sd, Shared &sh, CtaSmem &cs, W
         if (tid == 0) sh.nodefer = !bad;
         __syncthreads();
     }
-    if (M > 0 && sh.status == 0) {
-        for (long long k = tid; k < M; k += blockDim.x) sd.scr.gqueue[k] = -1;
+    if (M > 0 && vload(sh.w->status) == 0) {
+        for (long long k = gt; k < M; k += gstride) sd.scr.gqueue[k] = -1;
         /* dependency counters */
         for (int I = 0; I < ninst; I++) {
             const GRect r = gs.rect[I];
@@ -1572,7 +1646,7 @@ __device__ void graph_sweep(const fd_station_dev &sd, Shared &sh, CtaSmem &cs, W
             const int n = rect_n(r), nvf = r.vhi - r.vlo + 1;
             const unsigned myctx = sh.ctxm[r.face], myinn = sh.innm[r.face];
             const bool prev = sh.single && I > 0 && gs.rect[I - 1].layer == r.layer + fr.inner;
-            for (int j = tid; j < n; j += blockDim.x) {
+            for (int j = gt; j < n; j += gstride) {
                 const long long p = inst_node(sd, r, j);
                 unsigned cin = 0, c2 = 0, cx = 0;
                 if (sh.single) {
@@ -1603,36 +1677,37 @@ __device__ void graph_sweep(const fd_station_dev &sd, Shared &sh, CtaSmem &cs, W
                 sd.scr.gcnt[p] = cin | (c2 << 8) | (cx << 16);
             }
         }
-        __syncthreads();
+        csync(sh, 2);
         /* nodes whose inner block is final take their key now */
         for (int I = 0; I < ninst; I++) {
             const GRect r = gs.rect[I];
             const int n = rect_n(r);
-            for (int j = tid; j < n; j += blockDim.x) {
+            for (int j = gt; j < n; j += gstride) {
                 const long long p = inst_node(sd, r, j);
                 if ((sd.scr.gcnt[p] & 0xFFu) == 0u && ready_word(key_event(sd, sh, I, j, p))) graph_ready(sd, sh, r.face, p);
             }
         }
-        __syncthreads();
+        csync(sh, 3);
         FD_TOC(0, t0);
         FD_TIC(tw);
         run_walk(sd, sh, cs, ws, (int)M, nullptr, cn);
-        __syncthreads();
+        csync(sh, 4);
         FD_TOC(4, tw);
     }
     /* the small tables back to their empty state for the next sweep */
     {
-        const int nw = min(sh.nwait, FD_GWAIT_CAP), np = min(sh.npark, FD_GPARK_CAP), nr = min(sh.rqtail, FD_GRQ_CAP);
-        for (int k = tid; k < nw; k += blockDim.x) sd.scr.gwait[k] = make_int2(-1, -1);
-        for (int k = tid; k < np; k += blockDim.x) sd.scr.gpark[k] = make_int2(-1, -2);
-        for (int k = tid; k < nr; k += blockDim.x) sd.scr.grq[k] = -1;
+        const int nw = min(vload(sh.w->nwait), FD_GWAIT_CAP), np = min(vload(sh.w->npark), FD_GPARK_CAP);
+        const int nr = min(vload(sh.w->rqtail), FD_GRQ_CAP);
+        for (int k = gt; k < nw; k += gstride) sd.scr.gwait[k] = make_int2(-1, -1);
+        for (int k = gt; k < np; k += gstride) sd.scr.gpark[k] = make_int2(-1, -2);
+        for (int k = gt; k < nr; k += gstride) sd.scr.grq[k] = -1;
     }
     if (tid == 0) {
         /* the stencil state after the sweep: the record of its last writer */
         for (int I = ninst - 1; I >= 0; I--) {
-            const unsigned long long ek = sd.scr.ginst[I].exitkey;
+            const unsigned long long ek = vload(sd.scr.ginst[I].exitkey);
             if (ek) {
-                const float2 r = sd.scr.grec[inst_node(sd, gs.rect[I], (int)(ek & 0xffffffffu))];
+                const float2 r = __ldcg(&sd.scr.grec[inst_node(sd, gs.rect[I], (int)(ek & 0xffffffffu))]);
                 sh.carry_t0 = r.x;
                 sh.carry_t4 = r.y;
                 break;
@@ -1643,7 +1718,7 @@ __device__ void graph_sweep(const fd_station_dev &sd, Shared &sh, CtaSmem &cs, W
         sh.gsweeps++;
         sh.graph = 0;
     }
-    __syncthreads();
+    csync(sh, 5);
 }
 
 /* ---------------------------------------------------------------------------------------------- */
@@ -1686,28 +1761,46 @@ __device__ void init_field(const fd_station_dev &sd)
 /* ---------------------------------------------------------------------------------------------- */
 /* the sweep loop (src/sphfd.c:1008-5678)                                                          */
 
-__global__ void __launch_bounds__(FD_BLOCK, 1) fd_solve(const fd_station_dev *stations, int nst, int dag_smem_bytes)
+/* One station per cluster of csz CTAs (csz > 1 only for sweep graphs: face walks run in one CTA). */
+__global__ void __launch_bounds__(FD_BLOCK, 1) fd_solve(const fd_station_dev *stations, int nst, int dag_smem_bytes,
+                                                       int csz)
 {
     __shared__ Shared sh;
     extern __shared__ __align__(16) unsigned char fd_dyn_smem[];
     CtaSmem &cs = *reinterpret_cast<CtaSmem *>(fd_dyn_smem);
     WarpSmem &ws = reinterpret_cast<WarpSmem *>(fd_dyn_smem + kCtaSmemBytes)[threadIdx.x >> 5];
-    if ((int)blockIdx.x >= nst) return;
-    const fd_station_dev &sd = stations[blockIdx.x];
+    const int station = (int)blockIdx.x / csz;
+    if (station >= nst) return;   /* a whole cluster: its CTAs are consecutive */
+    const fd_station_dev &sd = stations[station];
     const int tid = threadIdx.x;
+    const int rank = csz > 1 ? (int)cooperative_groups::this_cluster().block_rank() : 0;
     unsigned long long t_start = 0;
     if (tid == 0) asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t_start));
     /* the dependency bytes of the station's largest face go to shared memory when they fit */
     unsigned char *dag = 2ll * sd.max_face_pad <= dag_smem_bytes ? fd_dyn_smem + kSmemBase : sd.scr.dag;
     const int gdim = sd.g.nx > sd.g.ny ? (sd.g.nx > sd.g.nz ? sd.g.nx : sd.g.nz) : (sd.g.ny > sd.g.nz ? sd.g.ny : sd.g.nz);
     const bool gok = sd.scr.gcnt && gdim <= FD_LMAX && (int)sizeof(GraphSmem) <= dag_smem_bytes;
-    if (gok) {
-        /* the sweep-graph tables start empty */
-        for (int k = tid; k < FD_GWAIT_CAP; k += blockDim.x) sd.scr.gwait[k] = make_int2(-1, -1);
-        for (int k = tid; k < FD_GPARK_CAP; k += blockDim.x) sd.scr.gpark[k] = make_int2(-1, -2);
-        for (int k = tid; k < FD_GRQ_CAP; k += blockDim.x) sd.scr.grq[k] = -1;
+    /* without sweep graphs the first CTA solves alone (the launcher does not ask for more) */
+    if (!gok && rank > 0) return;
+    sh.cs = gok ? csz : 1;
+    sh.rank = rank;
+    sh.w = sh.cs > 1 ? cooperative_groups::this_cluster().map_shared_rank(&sh.wl, 0) : &sh.wl;
+    if (tid == 0 && rank == 0) {
+        sh.wl.bar_count = 0;
+        sh.wl.bar_gen = 0;
     }
-    if (sd.init_mode == 0) init_field(sd);
+    /* once, before any CTA touches another's shared memory: every CTA of the cluster has started and
+     * the barrier counter is set; every CTA reaches this line */
+    if (sh.cs > 1) cooperative_groups::this_cluster().sync();
+    if (rank == 0) {
+        if (gok) {
+            /* the sweep-graph tables start empty */
+            for (int k = tid; k < FD_GWAIT_CAP; k += blockDim.x) sd.scr.gwait[k] = make_int2(-1, -1);
+            for (int k = tid; k < FD_GPARK_CAP; k += blockDim.x) sd.scr.gpark[k] = make_int2(-1, -2);
+            for (int k = tid; k < FD_GRQ_CAP; k += blockDim.x) sd.scr.grq[k] = -1;
+        }
+        if (sd.init_mode == 0) init_field(sd);
+    }
     for (int k = tid; k < FDN_NFACE * FDN_NTRIAL; k += blockDim.x) (&cs.desc[0][0])[k] = c_desc[k];
     if (tid == 0) {
         for (int f = 0; f < 6; f++) { sh.wall[f] = sd.wall[f]; sh.dflag[f] = sd.dflag[f]; }
@@ -1717,9 +1810,14 @@ __global__ void __launch_bounds__(FD_BLOCK, 1) fd_solve(const fd_station_dev *st
         sh.headpref = sd.headpref;
         sh.carry_t0 = sd.carry_t0;
         sh.carry_t4 = sd.carry_t4;
-        sh.status = 0;
-        sh.faces = sh.node_updates = sh.rounds = sh.deferred = 0;
-        for (int k = 0; k < 5; k++) sh.st[k] = 0;
+        if (rank == 0) {
+            sh.w->status = 0;
+            sh.w->rounds = sh.w->deferred = 0;
+            for (int k = 0; k < 5; k++) sh.w->st[k] = 0;
+            sh.w->nwait = 0;
+            sh.w->npark = 0;
+        }
+        sh.faces = sh.node_updates = 0;
         sh.sweeps = 0;
         for (int k = 0; k < 8; k++) sh.restart_wall[k] = 0;
         for (int k = 0; k < 6; k++) sh.cyc[k] = 0;
@@ -1731,23 +1829,21 @@ __global__ void __launch_bounds__(FD_BLOCK, 1) fd_solve(const fd_station_dev *st
         sh.single = 0;
         sh.nodefer = 0;
         sh.gfaces = 0;
-        sh.nwait = 0;
-        sh.npark = 0;
     }
-    __syncthreads();
+    csync(sh, 6);
     Counters cn;
     for (int k = 0; k < 5; k++) cn.n[k] = 0;
     const int nx = sd.g.nx, ny = sd.g.ny, nz = sd.g.nz;
     int guard_sweeps = 0;
-    while (sh.reverse > -1 && sh.status == 0) {
-        if (tid == 0) for (int k = 0; k < 8; k++) sh.headw[k] = 0;
-        __syncthreads();
+    while (sh.reverse > -1 && vload(sh.w->status) == 0) {
+        if (tid == 0 && rank == 0) for (int k = 0; k < 8; k++) sh.w->headw[k] = 0;
+        csync(sh, 7);
         FD_TIC(tsweep);
         const bool as_graph = sh.gok && (FD_GRAPH_FORWARD || sh.sweeps > 0);
         if (as_graph) graph_sweep(sd, sh, cs, ws, cn);
         while (!as_graph && sh.rad0
                && (sh.dflag[0] || sh.dflag[1] || sh.dflag[2] || sh.dflag[3] || sh.dflag[4] || sh.dflag[5])
-               && sh.status == 0) {
+               && sh.w->status == 0) {
             for (int face = 0; face < 6; face++) {
                 for (int ig = 1; ig <= sd.grow[face]; ig++) {
                     if (!sh.dflag[face]) continue;
@@ -1776,7 +1872,7 @@ __global__ void __launch_bounds__(FD_BLOCK, 1) fd_solve(const fd_station_dev *st
             if (sh.sweeps == 0) FD_TOC(5, tsweep);   /* profiling builds: the first sweep's cycles */
             sh.sweeps++;
             /* restart test (src/sphfd.c:5570-5676) */
-            const int *hw = sh.headw;
+            const int *hw = sh.w->headw;
             if (!hw[1] && !hw[2] && !hw[3] && !hw[4] && !hw[5] && !hw[6]) {
                 sh.reverse = 0;
             } else {
@@ -1798,21 +1894,22 @@ __global__ void __launch_bounds__(FD_BLOCK, 1) fd_solve(const fd_station_dev *st
             }
             sh.reverse--;
         }
-        __syncthreads();
-        if (++guard_sweeps > 1000000) { if (tid == 0) sh.status = 4; break; }
+        /* every CTA has read this sweep's head-wave counts before the next sweep clears them */
+        csync(sh, 8);
+        if (++guard_sweeps > 1000000) { if (tid == 0 && rank == 0) sh.w->status = 4; break; }
     }
     /* statistics */
-    for (int k = 0; k < 5; k++) atomicAdd(&sh.st[k], cn.n[k]);
-    __syncthreads();
-    if (tid == 0 && sd.stats) {
+    for (int k = 0; k < 5; k++) atomicAdd(&sh.w->st[k], cn.n[k]);
+    csync(sh, 9);
+    if (tid == 0 && rank == 0 && sd.stats) {
         fd_station_stats *o = sd.stats;
-        o->status = sh.status;
+        o->status = sh.w->status;
         o->sweeps = sh.sweeps;
         o->node_updates = sh.node_updates;
         o->faces = sh.faces;
-        o->rounds = sh.rounds;
-        o->deferred = sh.deferred;
-        for (int k = 0; k < 5; k++) o->stencils[k] = (int64_t)sh.st[k];
+        o->rounds = sh.w->rounds;
+        o->deferred = sh.w->deferred;
+        for (int k = 0; k < 5; k++) o->stencils[k] = (int64_t)sh.w->st[k];
         for (int k = 0; k < 8; k++) o->restart_wall[k] = sh.restart_wall[k];
         for (int k = 0; k < 6; k++) o->phase_cycles[k] = sh.cyc[k];
         unsigned long long t_end;
@@ -1821,6 +1918,9 @@ __global__ void __launch_bounds__(FD_BLOCK, 1) fd_solve(const fd_station_dev *st
         o->t_end_ns = (int64_t)t_end;
         o->pipelined_sweeps = (int32_t)sh.gsweeps;
     }
+    /* no CTA leaves while another may still read the first CTA's shared memory; every wait before
+     * this line is bounded, so every CTA reaches it */
+    if (sh.cs > 1) cooperative_groups::this_cluster().sync();
 }
 
 }  // namespace fdk
@@ -1834,22 +1934,48 @@ extern "C" cudaError_t fdk_launch_geo_build(int nx, int ny, int nz, double h, do
     return cudaGetLastError();
 }
 
-extern "C" cudaError_t fdk_launch_solve(const fd_station_dev *stations, int nst, long long max_face_pad,
+/* cluster: CTAs per station; 0 picks one CTA when the launch alone would not fill the GPU with
+ * stations, up to 8, as many as the SMs allow (1 keeps every station on one CTA) */
+extern "C" cudaError_t fdk_launch_solve(const fd_station_dev *stations, int nst, long long max_face_pad, int cluster,
                                         cudaStream_t stream)
 {
     if (nst <= 0) return cudaSuccess;
-    /* dynamic shared memory: the evaluation chunk, plus the face's dependency bytes if they fit */
-    int dev = 0, optin = 0;
+    /* dynamic shared memory: the warp areas, plus the sweep-graph tables or the face's dependency
+     * bytes, whichever is larger and fits */
+    int dev = 0, optin = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const long long base = (long long)fdk::kSmemBase;
     const long long graph = (long long)sizeof(fdk::GraphSmem);
     const long long dagb = 2 * max_face_pad > graph ? 2 * max_face_pad : graph;
     const long long bytes = base + dagb <= optin - 1024 ? base + dagb : (base + graph <= optin - 1024 ? base + graph : base);
-    const cudaError_t e = cudaFuncSetAttribute(fdk::fd_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    cudaError_t e = cudaFuncSetAttribute(fdk::fd_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
     if (e != cudaSuccess) return e;
-    fdk::fd_solve<<<nst, FD_BLOCK, (size_t)bytes, stream>>>(stations, nst, (int)(bytes - base));
-    return cudaGetLastError();
+    int cs = cluster;
+    if (cs <= 0) {
+        cs = 1;
+        if (bytes - base >= graph)
+            while (cs < 8 && (long long)nst * cs * 2 <= sms) cs *= 2;
+    }
+    if (cs == 1) {
+        fdk::fd_solve<<<nst, FD_BLOCK, (size_t)bytes, stream>>>(stations, nst, (int)(bytes - base), 1);
+        return cudaGetLastError();
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(nst * cs));
+    cfg.blockDim = dim3(FD_BLOCK);
+    cfg.dynamicSmemBytes = (size_t)bytes;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)cs;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    e = cudaLaunchKernelEx(&cfg, fdk::fd_solve, stations, nst, (int)(bytes - base), cs);
+    return e == cudaSuccess ? cudaGetLastError() : e;
 }
 
 /* slowness = 1/velocity, float division as the reference does it (src/sphfd.c:689-690) */

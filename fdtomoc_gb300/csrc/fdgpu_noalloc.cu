@@ -38,7 +38,7 @@
 extern "C" cudaError_t fdk_launch_geo_build(int nx, int ny, int nz, double h, double dq, double df, double z0r,
                                             const double *ysin, double *zrow, double *node, double *cell,
                                             cudaStream_t stream);
-extern "C" cudaError_t fdk_launch_solve(const fd_station_dev *stations, int nst, long long max_face_pad,
+extern "C" cudaError_t fdk_launch_solve(const fd_station_dev *stations, int nst, long long max_face_pad, int cluster,
                                         cudaStream_t stream);
 
 static __device__ __align__(256) unsigned char fd_noalloc_scratch[FDGPU_NOALLOC_SCRATCH_BYTES];
@@ -206,7 +206,7 @@ extern "C" int fdgpu_solve_noalloc(const fdgpu_station *st, const float *d_slown
         || cudaMemsetAsync(base + p.stats, 0, sizeof(fd_station_stats), cs) != cudaSuccess
         || cudaMemcpyAsync(base + p.station, &d, sizeof d, cudaMemcpyHostToDevice, cs) != cudaSuccess)
         return FDGPU_ECUDA;
-    if (fdk_launch_solve(reinterpret_cast<const fd_station_dev *>(base + p.station), 1, p.max_face_pad, cs)
+    if (fdk_launch_solve(reinterpret_cast<const fd_station_dev *>(base + p.station), 1, p.max_face_pad, 1, cs)
         != cudaSuccess)
         return FDGPU_ECUDA;
     fd_station_stats hs;

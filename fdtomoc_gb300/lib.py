@@ -70,6 +70,7 @@ def load() -> C.CDLL:
         lib.fdgpu_strerror.restype = C.c_char_p
         lib.fdgpu_last_error.argtypes = [P]
         lib.fdgpu_last_error.restype = C.c_char_p
+        lib.fdgpu_set_cluster.argtypes = [P, C.c_int]
         lib.fdgpu_station_from_par.argtypes = [C.c_int, C.POINTER(C.c_char_p), C.POINTER(Station), C.c_char_p,
                                                C.c_size_t, C.c_char_p, C.c_size_t]
         lib.fdgpu_solve_host.argtypes = [P, C.c_int, C.POINTER(Station), C.POINTER(C.c_float), C.c_int, C.c_int,
@@ -115,6 +116,10 @@ class Context:
         self.lib = load()
         self.ptr = C.c_void_p()
         _check(self.lib.fdgpu_create(device, C.byref(self.ptr)))
+
+    def set_cluster(self, ctas_per_station: int):
+        """CTAs per station in later solves (0: automatic)."""
+        _check(self.lib.fdgpu_set_cluster(self.ptr, ctas_per_station))
 
     def close(self):
         if self.ptr:
