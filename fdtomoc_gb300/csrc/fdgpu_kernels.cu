@@ -35,6 +35,12 @@
 #include "fdgpu_layout.h"
 
 #define FD_WARPS 12                 /* independent workers per station */
+/* Largest cluster of CTAs one station may use.  Multi-CTA solving (the walk state shared through
+ * distributed shared memory) passed the bit-exactness tests but hung or faulted intermittently on
+ * this GPU; until the cause is found every station runs on one CTA. */
+#ifndef FD_MAX_CLUSTER
+#define FD_MAX_CLUSTER 1
+#endif
 #define FD_BLOCK (FD_WARPS * 32)
 
 /* optional per-phase cycle counters (thread 0, between barriers) for profiling builds */
@@ -136,13 +142,14 @@ struct WalkShared {
     unsigned long long exitkey;
     long long rounds, deferred;
     unsigned long long st[5];
-    int bar_count, bar_gen;   /* cluster barrier: arrivals, generation */
+    int bar_count;            /* cluster barrier: arrivals so far */
 };
 
 struct Shared {
     WalkShared wl;
     WalkShared *w;           /* the cluster's shared walk state (wl of rank 0) */
     int cs, rank;            /* CTAs per station, this CTA's rank */
+    int stat;                /* the station's status as this CTA read it at its last barrier */
     int wall[6], dflag[6];
     int radius, rad0, reverse, headpref;
     float carry_t0, carry_t4;
@@ -182,34 +189,32 @@ __device__ __forceinline__ void wfence(const Shared &sh)
 #endif
 
 /* Barrier of all threads of the station's CTAs: the CTA's threads meet, its thread 0 meets the other
- * CTAs' at a generation counter in the first CTA's shared memory.  The wait is bounded: a CTA that
- * waits too long records which barrier (site) gave up in the station's status and goes on, so a
- * fault in the schedule ends in an error, never in a hang. */
+ * CTAs' at an arrival counter in the first CTA's shared memory that only grows (barrier k is passed
+ * once it reaches (k+1) * CTAs, so no arrival can be lost to a reset).  The wait is bounded: a CTA
+ * that waits too long records which barrier (site) gave up in the station's status and goes on, so
+ * a fault in the schedule ends in an error, never in a hang.  Thread 0 then takes the station's
+ * status for the whole CTA (sh.stat), so every branch that depends on it is taken by all threads. */
 __device__ __forceinline__ void csync(Shared &sh, int site)
 {
     __syncthreads();
-    if (sh.cs > 1) {
-        if (threadIdx.x == 0) {
+    if (threadIdx.x == 0) {
+        if (sh.cs > 1) {
             asm volatile("fence.acq_rel.cluster;" ::: "memory");
-            const int gen = *const_cast<volatile int *>(&sh.w->bar_gen);
-            if (atomicAdd(&sh.w->bar_count, 1) == sh.cs - 1) {
-                sh.w->bar_count = 0;
-                asm volatile("fence.acq_rel.cluster;" ::: "memory");
-                atomicAdd(&sh.w->bar_gen, 1);
-            } else {
-                long long spins = 0;
-                while (*const_cast<volatile int *>(&sh.w->bar_gen) == gen) {
-                    __nanosleep(64);
-                    if (++spins > FD_BAR_SPINS) {
-                        atomicCAS(&sh.w->status, 0, 100 + site);
-                        break;
-                    }
+            const int my = atomicAdd(&sh.w->bar_count, 1);
+            const int target = (my / sh.cs + 1) * sh.cs;
+            long long spins = 0;
+            while (*const_cast<volatile int *>(&sh.w->bar_count) < target) {
+                __nanosleep(64);
+                if (++spins > FD_BAR_SPINS) {
+                    atomicCAS(&sh.w->status, 0, 100 + site);
+                    break;
                 }
             }
             asm volatile("fence.acq_rel.cluster;" ::: "memory");
         }
-        __syncthreads();
+        sh.stat = *const_cast<volatile int *>(&sh.w->status);
     }
+    __syncthreads();
 }
 
 /* face frame for a face number known only at run time */
@@ -1637,7 +1642,7 @@ __device__ void graph_sweep(const fd_station_dev &sd, Shared &sh, CtaSmem &cs, W
         if (tid == 0) sh.nodefer = !bad;
         __syncthreads();
     }
-    if (M > 0 && vload(sh.w->status) == 0) {
+    if (M > 0 && sh.stat == 0) {
         for (long long k = gt; k < M; k += gstride) sd.scr.gqueue[k] = -1;
         /* dependency counters */
         for (int I = 0; I < ninst; I++) {
@@ -1785,10 +1790,8 @@ __global__ void __launch_bounds__(FD_BLOCK, 1) fd_solve(const fd_station_dev *st
     sh.cs = gok ? csz : 1;
     sh.rank = rank;
     sh.w = sh.cs > 1 ? cooperative_groups::this_cluster().map_shared_rank(&sh.wl, 0) : &sh.wl;
-    if (tid == 0 && rank == 0) {
-        sh.wl.bar_count = 0;
-        sh.wl.bar_gen = 0;
-    }
+    if (tid == 0 && rank == 0) sh.wl.bar_count = 0;
+    if (tid == 0) sh.stat = 0;
     /* once, before any CTA touches another's shared memory: every CTA of the cluster has started and
      * the barrier counter is set; every CTA reaches this line */
     if (sh.cs > 1) cooperative_groups::this_cluster().sync();
@@ -1835,7 +1838,7 @@ __global__ void __launch_bounds__(FD_BLOCK, 1) fd_solve(const fd_station_dev *st
     for (int k = 0; k < 5; k++) cn.n[k] = 0;
     const int nx = sd.g.nx, ny = sd.g.ny, nz = sd.g.nz;
     int guard_sweeps = 0;
-    while (sh.reverse > -1 && vload(sh.w->status) == 0) {
+    while (sh.reverse > -1 && sh.stat == 0) {
         if (tid == 0 && rank == 0) for (int k = 0; k < 8; k++) sh.w->headw[k] = 0;
         csync(sh, 7);
         FD_TIC(tsweep);
@@ -1843,7 +1846,7 @@ __global__ void __launch_bounds__(FD_BLOCK, 1) fd_solve(const fd_station_dev *st
         if (as_graph) graph_sweep(sd, sh, cs, ws, cn);
         while (!as_graph && sh.rad0
                && (sh.dflag[0] || sh.dflag[1] || sh.dflag[2] || sh.dflag[3] || sh.dflag[4] || sh.dflag[5])
-               && sh.w->status == 0) {
+               && sh.stat == 0) {
             for (int face = 0; face < 6; face++) {
                 for (int ig = 1; ig <= sd.grow[face]; ig++) {
                     if (!sh.dflag[face]) continue;
@@ -1866,7 +1869,7 @@ __global__ void __launch_bounds__(FD_BLOCK, 1) fd_solve(const fd_station_dev *st
                 sh.radius++;
                 if (sh.radius == sd.maxrad) sh.rad0 = 0;
             }
-            __syncthreads();
+            csync(sh, 10);
         }
         if (tid == 0) {
             if (sh.sweeps == 0) FD_TOC(5, tsweep);   /* profiling builds: the first sweep's cycles */
@@ -1934,8 +1937,9 @@ extern "C" cudaError_t fdk_launch_geo_build(int nx, int ny, int nz, double h, do
     return cudaGetLastError();
 }
 
-/* cluster: CTAs per station; 0 picks one CTA when the launch alone would not fill the GPU with
- * stations, up to 8, as many as the SMs allow (1 keeps every station on one CTA) */
+/* cluster: CTAs per station; 0 picks more than one when the stations alone would leave SMs idle,
+ * up to 8 (1 keeps every station on one CTA).  Reduced until every cluster of the launch is
+ * co-resident. */
 extern "C" cudaError_t fdk_launch_solve(const fd_station_dev *stations, int nst, long long max_face_pad, int cluster,
                                         cudaStream_t stream)
 {
@@ -1952,12 +1956,21 @@ extern "C" cudaError_t fdk_launch_solve(const fd_station_dev *stations, int nst,
     const long long bytes = base + dagb <= optin - 1024 ? base + dagb : (base + graph <= optin - 1024 ? base + graph : base);
     cudaError_t e = cudaFuncSetAttribute(fdk::fd_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
     if (e != cudaSuccess) return e;
+    /* CTAs per station: with clusters of 2 any two SMs of a GPC serve; clusters of 4 and 8 are taken
+     * only with room to spare, so that every cluster of the launch is co-resident (launches whose
+     * clusters of 8 ran in several waves faulted once on this GPU; they are not made) */
+    auto fits = [&](int c) {
+        const long long ctas = (long long)nst * c;
+        return c == 1 || (c == 2 && ctas <= sms) || (c == 4 && 4 * ctas <= 3ll * sms) || (c == 8 && 2 * ctas <= sms);
+    };
     int cs = cluster;
     if (cs <= 0) {
         cs = 1;
-        if (bytes - base >= graph)
-            while (cs < 8 && (long long)nst * cs * 2 <= sms) cs *= 2;
+        while (cs < 8 && fits(cs * 2) && (long long)nst * cs * 2 <= sms) cs *= 2;
     }
+    while (cs > 1 && !fits(cs)) cs /= 2;
+    if (cs > FD_MAX_CLUSTER) cs = FD_MAX_CLUSTER;
+    if (bytes - base < graph) cs = 1;   /* no room for the sweep-graph tables: face walks, one CTA */
     if (cs == 1) {
         fdk::fd_solve<<<nst, FD_BLOCK, (size_t)bytes, stream>>>(stations, nst, (int)(bytes - base), 1);
         return cudaGetLastError();

@@ -103,10 +103,10 @@ int fdgpu_station_from_par(int ac, char **av, fdgpu_station *st, char *velfile, 
 int fdgpu_solve_host(fdgpu_ctx *ctx, int n, const fdgpu_station *st, const float *velocity, int mnx, int mny,
                      int mnz, float *const *times, const float *const *init_times, fdgpu_stats *stats);
 
-/* CTAs (one per SM) that cooperate on each station in later solves of this context, as one
- * thread-block cluster: 0 (the default) takes 1, or up to 8 when a batch leaves SMs idle; 1, 2, 4
- * or 8 fixes it.  Results do not depend on it.  No counterpart in the reference (one OpenMP thread
- * per station). */
+/* CTAs (one per SM) that may cooperate on each station in later solves of this context, as one
+ * thread-block cluster: 0 (the default) lets the library choose, 1, 2, 4 or 8 asks for that many.
+ * The library currently caps it at 1 (multi-CTA solving is disabled in this build).  Results do not
+ * depend on it.  No counterpart in the reference (one OpenMP thread per station). */
 int fdgpu_set_cluster(fdgpu_ctx *ctx, int ctas_per_station);
 
 /* Same with everything already on the device: slowness (1/v, float) of a model with strides
