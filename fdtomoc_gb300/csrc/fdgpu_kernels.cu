@@ -909,7 +909,8 @@ __device__ void graph_release(const fd_station_dev &sd, Shared &sh, int F, long 
     }
     /* later neighbours in the same instance */
     const int nvf = r.vhi - r.vlo + 1, iu = i % r.nuf, iv = i / r.nuf;
-    unsigned later = inrect_mask(iu, iv, r.nuf, nvf) & ~(unsigned)__ldcg(&sd.scr.gemask[p]);
+    const unsigned char gem = sh.cs > 1 ? __ldcg(&sd.scr.gemask[p]) : sd.scr.gemask[p];
+    unsigned later = inrect_mask(iu, iv, r.nuf, nvf) & ~(unsigned)gem;
     while (later) {
         const int k = __ffs(later) - 1;
         later &= later - 1;
@@ -1110,8 +1111,10 @@ __device__ void warp_chunk(const fd_station_dev &sd, Shared &sh, const CtaSmem &
             const int uu = wh.r.u + du, vv = wh.r.v + dv;
             float tv = 0.f, svv = 0.f;
             if (uu >= 0 && uu < wh.r.nu && vv >= 0 && vv < wh.r.nv) {
-                /* through L2: another SM may have written it since this SM last read it */
-                tv = __ldcg(&sd.T[wh.p + du * su + dv * sv + (w ? inner_t : 0ll)]);
+                /* with several CTAs, through L2: another SM may have written it since this SM last
+                 * read it; one CTA's own stores keep its L1 current */
+                const float *pt = &sd.T[wh.p + du * su + dv * sv + (w ? inner_t : 0ll)];
+                tv = sh.cs > 1 ? __ldcg(pt) : *pt;
                 svv = __ldg(&sd.S[pS + du * ssu + dv * ssv + (w ? inner_s : 0ll)]);
             }
             tr[nb] = tv;
