@@ -51,7 +51,7 @@ def build(force: bool = False, verbose: bool = False, defines=(), lib_path: str 
     os.makedirs(os.path.dirname(EXE), exist_ok=True)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
     headers.append(os.path.join(ROOT, "include", "fdgpu.h"))
-    units = [("fdgpu_kernels.cu", []), ("fdgpu_host.cpp", []), ("fdgpu_noalloc.cu", [])]
+    units = [("fdgpu_kernels.cu", []), ("fdgpu_host.cpp", []), ("fdgpu_noalloc.cu", []), ("fdgpu_serve.cpp", [])]
     objs = []
     jobs = []
     for src, extra in units:
@@ -65,7 +65,7 @@ def build(force: bool = False, verbose: bool = False, defines=(), lib_path: str 
             if verbose:
                 print(r.stderr)
     if force or _stale(lib_out, objs):
-        _run([nvcc] + ARCH + ["-shared", "-cudart", "static", "-o", lib_out] + objs)
+        _run([nvcc] + ARCH + ["-shared", "-cudart", "static", "-o", lib_out] + objs + ["-lpthread"])
     if lib_path:
         return lib_out
     main = os.path.join(CSRC, "sphfd_main.cpp")

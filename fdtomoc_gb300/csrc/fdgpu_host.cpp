@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "fdgpu_layout.h"
+#include "fdgpu_station.h"
 
 extern "C" cudaError_t fdk_launch_geo_build(int nx, int ny, int nz, double h, double dq, double df, double z0r,
                                             const double *ysin, double *zrow, double *node, double *cell,
@@ -112,8 +113,8 @@ double glath(double hlat, double depth_km, double *radius_km)
     return std::atan2(zp, xp);
 }
 
-double qc(const fdgpu_station &s, int y) { return s.y0 + s.dq * (double)y; }
-double fc(const fdgpu_station &s, int x) { return s.x0 + s.df * (double)x; }
+using fdh::qc;
+using fdh::fc;
 double rc(const fdgpu_station &s, int z) { return s.z0r - s.h * (double)z; }
 
 Geo *geometry(fdgpu_ctx *ctx, const fdgpu_station &s, int *status)
@@ -123,7 +124,7 @@ Geo *geometry(fdgpu_ctx *ctx, const fdgpu_station &s, int *status)
     if (it != ctx->geos.end()) return it->second.get();
     auto g = std::make_unique<Geo>();
     std::vector<double> ys(s.ny);
-    for (int y = 0; y < s.ny; y++) ys[y] = std::sin(qc(s, y));   /* sin() per call in the reference */
+    fdh::ysin_table(s, ys.data());
     cudaError_t e;
     if ((e = g->ysin.ensure(sizeof(double) * s.ny)) || (e = g->zrow.ensure(sizeof(double) * FD_Z_N * s.nz))
         || (e = g->node.ensure(sizeof(double) * FD_N_N * (size_t)s.nz * s.ny))
@@ -145,80 +146,8 @@ Geo *geometry(fdgpu_ctx *ctx, const fdgpu_station &s, int *status)
     return raw;
 }
 
-/* initial box of a point source (src/sphfd.c:766-825), in face order z1 z2 x2 x1 y1 y2 */
-void point_box(const fdgpu_station &s, int wall[6], int dflag[6])
-{
-    const int nc = s.ncube;
-    for (int f = 0; f < 6; f++) dflag[f] = 1;
-    if (s.xs > nc) wall[3] = s.xs - (nc + 1); else { wall[3] = -1; dflag[3] = 0; }
-    if (s.xs < s.nx - (nc + 1)) wall[2] = s.xs + (nc + 1); else { wall[2] = s.nx; dflag[2] = 0; }
-    if (s.ys > nc) wall[4] = s.ys - (nc + 1); else { wall[4] = -1; dflag[4] = 0; }
-    if (s.ys < s.ny - (nc + 1)) wall[5] = s.ys + (nc + 1); else { wall[5] = s.ny; dflag[5] = 0; }
-    if (s.zs > nc) wall[0] = s.zs - (nc + 1); else { wall[0] = -1; dflag[0] = 0; }
-    if (s.zs < s.nz - (nc + 1)) wall[1] = s.zs + (nc + 1); else { wall[1] = s.nz; dflag[1] = 0; }
-}
-
-/* box = one whole model wall (src/sphfd.c:877-926 and :5623-5674) */
-void wall_box(const fdgpu_station &s, int srcwall, int wall[6], int dflag[6])
-{
-    for (int f = 0; f < 6; f++) dflag[f] = 1;
-    if (srcwall == 1) wall[2] = 1; else { wall[2] = s.nx; dflag[2] = 0; }
-    if (srcwall == 2) wall[3] = s.nx - 2; else { wall[3] = -1; dflag[3] = 0; }
-    if (srcwall == 3) wall[5] = 1; else { wall[5] = s.ny; dflag[5] = 0; }
-    if (srcwall == 4) wall[4] = s.ny - 2; else { wall[4] = -1; dflag[4] = 0; }
-    if (srcwall == 5) wall[1] = 1; else { wall[1] = s.nz; dflag[1] = 0; }
-    if (srcwall == 6) wall[0] = s.nz - 2; else { wall[0] = -1; dflag[0] = 0; }
-}
-
-/* preferred restart wall from the initial box (src/sphfd.c:977-1003) */
-int resolve_headpref(const fdgpu_station &s, const int wall[6], int headpref)
-{
-    if (headpref <= 0) return headpref;
-    const int x1 = wall[3], x2 = wall[2], y1 = wall[4], y2 = wall[5], z1 = wall[0], z2 = wall[1];
-    long long head = (long long)s.nx * s.ny * s.nz;
-    if (s.nx > 5 && x2 <= head) { headpref = 2; head = x2; }
-    if (s.nx > 5 && (s.nx - 1 - x1) <= head) { headpref = 1; head = s.nx - 1 - x1; }
-    if (s.ny > 5 && y2 <= head) { headpref = 4; head = y2; }
-    if (s.ny > 5 && (s.ny - 1 - y1) <= head) { headpref = 3; head = s.ny - 1 - y1; }
-    if (s.nz > 5 && z2 <= head) { headpref = 6; head = z2; }
-    if (s.nz > 5 && (s.nz - 1 - z1) <= head) { headpref = 5; head = s.nz - 1 - z1; }
-    return headpref;
-}
-
-long long max_face(const fdgpu_station &s)
-{
-    return std::max({(long long)s.nx * s.ny, (long long)s.nx * s.nz, (long long)s.ny * s.nz});
-}
-
-constexpr size_t kScratchPerPoint = 8 + 4 + 4 + 4 + 8 + 4 + 2;
-/* sweep-graph arrays per grid node: stencil-state record, counter, queue, earlier-neighbour byte;
- * then the face instances, wait pairs, parked points and resume queue */
-constexpr size_t kGraphPerNode = 8 + 4 + 4 + 1;
-
-size_t graph_node_bytes(size_t nn) { return (nn * kGraphPerNode + 255) & ~(size_t)255; }
-
-size_t graph_bytes(const fdgpu_station &s)
-{
-    const size_t nn = (size_t)s.nx * s.ny * s.nz;
-    const size_t ninst = (size_t)s.nx + s.ny + s.nz + 8;
-    return graph_node_bytes(nn) + ((ninst * sizeof(fd_ginst) + 255) & ~(size_t)255)
-           + 8 * (size_t)FD_GWAIT_CAP + 8 * (size_t)FD_GPARK_CAP + 4 * (size_t)FD_GRQ_CAP;
-}
-
-int check_station(const fdgpu_station &s)
-{
-    if (s.nx < 2 || s.ny < 2 || s.nz < 2 || !(s.h > 0) || !(s.dq != 0) || !(s.df != 0)) return FDGPU_EINVAL;
-    if ((long long)s.nx * s.ny > 0x7fffffffLL / 2 || max_face(s) > (1LL << 30)) return FDGPU_EINVAL;
-    if (s.srctype == 1) {
-        if (s.xs < 0 || s.ys < 0 || s.zs < 0 || s.xs > s.nx - 1 || s.ys > s.ny - 1 || s.zs > s.nz - 1) return FDGPU_ESOURCE;
-        if (s.ncube < 0 || s.ncube > 64) return FDGPU_EINVAL;
-    } else if (s.srctype == 2 || s.srctype == 3) {
-        if (s.srcwall < 1 || s.srcwall > 6) return FDGPU_EPAR;
-    } else {
-        return FDGPU_EPAR;
-    }
-    return FDGPU_OK;
-}
+using fdh::check_station;
+using fdh::max_face;
 
 }  // namespace
 
@@ -264,7 +193,7 @@ extern "C" const char *fdgpu_strerror(int s)
     case FDGPU_ESOURCE: return "source outside the grid";
     case FDGPU_ESCHED: return "a schedule check of the solve failed (fdgpu_stats.detail says which)";
     case FDGPU_ENODEV: return "no CUDA device";
-    case FDGPU_ETOOBIG: return "problem exceeds the static scratch of the no-allocation entry point";
+    case FDGPU_ETOOBIG: return "problem exceeds the memory the entry point may use";
     default: return "unknown status";
     }
 }
@@ -317,91 +246,30 @@ extern "C" int fdgpu_solve_device(fdgpu_ctx *ctx, int n, const fdgpu_station *st
         if (!d_times[k] || ((uintptr_t)d_times[k] & 3u) != 0) return FDGPU_EINVAL;
         if (st[k].srctype != 1 && !times_initialised) return FDGPU_EINVAL;
     }
-    /* scratch and per-station records */
+    /* scratch and per-station records: per station, face scratch, then the sweep-graph arrays */
     std::vector<size_t> off(n + 1, 0);
-    /* per station: face scratch, then the sweep-graph arrays */
-    auto nodes = [&](int k) { return (size_t)st[k].nx * st[k].ny * st[k].nz; };
-    for (int k = 0; k < n; k++)
-        off[k + 1] = off[k] + ((((size_t)max_face(st[k]) + 16) * kScratchPerPoint + 255) & ~(size_t)255)
-                     + graph_bytes(st[k]);
+    for (int k = 0; k < n; k++) off[k + 1] = off[k] + fdh::face_bytes(st[k]) + fdh::graph_bytes(st[k]);
     FD_CU(ctx, ctx->scratch.ensure(off[n]));
     FD_CU(ctx, ctx->stations.ensure(sizeof(fd_station_dev) * n));
     FD_CU(ctx, ctx->stats.ensure(sizeof(fd_station_stats) * n));
-    int maxw = 0;
-    for (int k = 0; k < n; k++) maxw = std::max(maxw, 2 * st[k].ncube + 1);
-    FD_CU(ctx, ctx->trig.ensure(sizeof(double) * 4 * (size_t)maxw * n + 8));
+    int maxt = 0;
+    for (int k = 0; k < n; k++) maxt = std::max(maxt, fdh::box_trig_count(st[k]));
+    FD_CU(ctx, ctx->trig.ensure(sizeof(double) * (size_t)maxt * n + 8));
     std::vector<fd_station_dev> hs(n);
     long long max_pad = 16;
-    std::vector<double> trig(4 * (size_t)maxw * n, 0.0);
+    std::vector<double> trig((size_t)maxt * n, 0.0);
     for (int k = 0; k < n; k++) {
         const fdgpu_station &s = st[k];
         int status = 0;
         Geo *g = geometry(ctx, s, &status);
         if (!g) return status;
-        fd_station_dev &d = hs[k];
-        std::memset(&d, 0, sizeof d);
-        d.g.nx = s.nx; d.g.ny = s.ny; d.g.nz = s.nz;
-        d.g.h = s.h; d.g.inv_h = 1.0 / s.h; d.g.dq = s.dq; d.g.df = s.df; d.g.is_h = 1.0 / (s.h * s.h);
-        d.g.zrow = g->zrow.as<double>(); d.g.ysin = g->ysin.as<double>();
-        d.g.node = g->node.as<double>(); d.g.cell = g->cell.as<double>();
-        d.T = d_times[k];
-        d.S = slowness + (long long)s.oz * s_sz + (long long)s.oy * s_sy + s.ox;
-        d.s_sy = s_sy; d.s_sz = s_sz;
-        if (s.srctype == 1) point_box(s, d.wall, d.dflag);
-        else wall_box(s, s.srcwall, d.wall, d.dflag);
-        const int grow[6] = {s.kminus, s.kplus, s.iplus, s.iminus, s.jminus, s.jplus};
-        for (int f = 0; f < 6; f++) d.grow[f] = grow[f];
-        d.radius = s.srctype == 1 ? s.ncube : 1;
-        d.reverse = s.reverse;
-        d.headpref = resolve_headpref(s, d.wall, s.headpref);
-        d.maxrad = s.maxrad;
-        d.carry_t0 = 0.f; d.carry_t4 = 0.f;
-        d.init_mode = (s.srctype == 1 && !times_initialised) ? 0 : 1;
-        d.xs = s.xs; d.ys = s.ys; d.zs = s.zs; d.ncube = s.ncube;
-        /* Cartesian source point (src/sphfd.c:727-729) and the box's trig values (:740-745) */
-        const double fxss = s.src_geo[0], fyss = s.src_geo[1], fzss = s.src_geo[2];
-        d.src_xyz[0] = fzss * std::cos(fyss);
-        d.src_xyz[1] = fzss * std::sin(fyss) * std::cos(fxss);
-        d.src_xyz[2] = fzss * std::sin(fyss) * std::sin(fxss);
-        const int w = 2 * s.ncube + 1;
-        double *tg = trig.data() + 4 * (size_t)maxw * k;
-        for (int j = 0; j < w; j++) {
-            const double q = qc(s, s.ys - s.ncube + j), f = fc(s, s.xs - s.ncube + j);
-            tg[2 * j] = std::cos(q);
-            tg[2 * j + 1] = std::sin(q);
-            tg[2 * w + 2 * j] = std::cos(f);
-            tg[2 * w + 2 * j + 1] = std::sin(f);
-        }
-        d.box_trig = ctx->trig.as<double>() + 4 * (size_t)maxw * k;
+        const fdh::GeoPtrs gp{g->ysin.as<double>(), g->zrow.as<double>(), g->node.as<double>(), g->cell.as<double>()};
+        fdh::box_trig(s, trig.data() + (size_t)maxt * k);
         char *base = ctx->scratch.as<char>() + off[k];
-        const size_t m = (size_t)max_face(s);
-        d.scr.key = reinterpret_cast<unsigned long long *>(base);
-        d.scr.rec = reinterpret_cast<float2 *>(base + 8 * m);
-        d.scr.pst = reinterpret_cast<int *>(base + 16 * m);
-        d.scr.queue = reinterpret_cast<int *>(base + 20 * m);
-        d.scr.rq = reinterpret_cast<int *>(base + 24 * m);
-        d.scr.dag = reinterpret_cast<unsigned char *>(base + 32 * m);
-        {
-            /* 8-byte records first, then the 4-byte arrays, then the bytes */
-            char *pb = base + ((((size_t)m + 16) * kScratchPerPoint + 255) & ~(size_t)255);
-            const size_t nn = nodes(k);
-            d.scr.grec = reinterpret_cast<float2 *>(pb);
-            d.scr.gcnt = reinterpret_cast<unsigned *>(pb + 8 * nn);
-            d.scr.gqueue = reinterpret_cast<int *>(pb + 12 * nn);
-            d.scr.gemask = reinterpret_cast<unsigned char *>(pb + 16 * nn);
-            char *tb = pb + graph_node_bytes(nn);
-            d.scr.ginst_cap = s.nx + s.ny + s.nz + 8;
-            d.scr.ginst = reinterpret_cast<fd_ginst *>(tb);
-            tb += ((size_t)d.scr.ginst_cap * sizeof(fd_ginst) + 255) & ~(size_t)255;
-            d.scr.gwait = reinterpret_cast<int2 *>(tb);
-            tb += 8 * (size_t)FD_GWAIT_CAP;
-            d.scr.gpark = reinterpret_cast<int2 *>(tb);
-            tb += 8 * (size_t)FD_GPARK_CAP;
-            d.scr.grq = reinterpret_cast<int *>(tb);
-        }
-        d.max_face_pad = ((long long)m + 15) & ~15LL;
-        max_pad = std::max(max_pad, d.max_face_pad);
-        d.stats = ctx->stats.as<fd_station_stats>() + k;
+        fdh::fill_station(hs[k], s, gp, d_times[k], slowness, s_sy, s_sz,
+                          (s.srctype == 1 && !times_initialised) ? 0 : 1, base, base + fdh::face_bytes(s),
+                          ctx->trig.as<double>() + (size_t)maxt * k, ctx->stats.as<fd_station_stats>() + k);
+        max_pad = std::max(max_pad, hs[k].max_face_pad);
     }
     FD_CU(ctx, cudaMemcpyAsync(ctx->trig.p, trig.data(), sizeof(double) * trig.size(), cudaMemcpyHostToDevice, cs));
     FD_CU(ctx, cudaMemcpyAsync(ctx->stations.p, hs.data(), sizeof(fd_station_dev) * n, cudaMemcpyHostToDevice, cs));
@@ -411,22 +279,7 @@ extern "C" int fdgpu_solve_device(fdgpu_ctx *ctx, int n, const fdgpu_station *st
     FD_CU(ctx, cudaStreamSynchronize(cs));
     int rc = FDGPU_OK;
     for (int k = 0; k < n; k++) {
-        if (stats) {
-            fdgpu_stats &o = stats[k];
-            o.status = hst[k].status ? FDGPU_ESCHED : FDGPU_OK;
-            o.sweeps = hst[k].sweeps;
-            o.node_updates = hst[k].node_updates;
-            o.faces = hst[k].faces;
-            o.rounds = hst[k].rounds;
-            o.deferred = hst[k].deferred;
-            for (int j = 0; j < 5; j++) o.stencils[j] = hst[k].stencils[j];
-            for (int j = 0; j < 8; j++) o.restart_wall[j] = hst[k].restart_wall[j];
-            for (int j = 0; j < 6; j++) o.phase_cycles[j] = hst[k].phase_cycles[j];
-            o.t_start_ns = hst[k].t_start_ns;
-            o.t_end_ns = hst[k].t_end_ns;
-            o.pipelined_sweeps = hst[k].pipelined_sweeps;
-            o.detail = hst[k].status;
-        }
+        if (stats) fdh::copy_stats(stats[k], hst[k]);
         if (hst[k].status && rc == FDGPU_OK) rc = FDGPU_ESCHED;
     }
     return rc;

@@ -703,6 +703,10 @@ struct GraphSmem {
     GRect rect[FD_IMAX];
 };
 
+/* the warp areas and the sweep-graph tables fit one CTA's 227 KB, with 2 KB left for the static
+ * shared memory of fd_solve */
+static_assert(kSmemBase + sizeof(GraphSmem) + 2048 <= 227 * 1024, "shared memory of one CTA");
+
 __device__ __forceinline__ GraphSmem &gsmem(const Shared &sh) { return *reinterpret_cast<GraphSmem *>(sh.gsm); }
 
 /* Neighbour offsets (dx,dy,dz) are numbered k = (dz+1)*9 + (dy+1)*3 + (dx+1), 13 being the node
@@ -1769,17 +1773,13 @@ __device__ void init_field(const fd_station_dev &sd)
 /* ---------------------------------------------------------------------------------------------- */
 /* the sweep loop (src/sphfd.c:1008-5678)                                                          */
 
-/* One station per cluster of csz CTAs (csz > 1 only for sweep graphs: face walks run in one CTA). */
-__global__ void __launch_bounds__(FD_BLOCK, 1) fd_solve(const fd_station_dev *stations, int nst, int dag_smem_bytes,
-                                                       int csz)
+/* The solve of one station by this CTA, or by this cluster of csz CTAs (csz > 1 only for sweep
+ * graphs: face walks run in one CTA).  sd is the station record in this CTA's shared memory. */
+__device__ __forceinline__ void solve_station(const fd_station_dev &sd, int dag_smem_bytes, int csz, Shared &sh)
 {
-    __shared__ Shared sh;
     extern __shared__ __align__(16) unsigned char fd_dyn_smem[];
     CtaSmem &cs = *reinterpret_cast<CtaSmem *>(fd_dyn_smem);
     WarpSmem &ws = reinterpret_cast<WarpSmem *>(fd_dyn_smem + kCtaSmemBytes)[threadIdx.x >> 5];
-    const int station = (int)blockIdx.x / csz;
-    if (station >= nst) return;   /* a whole cluster: its CTAs are consecutive */
-    const fd_station_dev &sd = stations[station];
     const int tid = threadIdx.x;
     const int rank = csz > 1 ? (int)cooperative_groups::this_cluster().block_rank() : 0;
     unsigned long long t_start = 0;
@@ -1929,6 +1929,88 @@ __global__ void __launch_bounds__(FD_BLOCK, 1) fd_solve(const fd_station_dev *st
     if (sh.cs > 1) cooperative_groups::this_cluster().sync();
 }
 
+/* a station record copied into shared memory by the whole CTA; cache-volatile loads, because a
+ * serving session rewrites a record slot between the requests this SM reads from it */
+__device__ __forceinline__ void load_record(fd_station_dev &dst, const fd_station_dev *src)
+{
+    static_assert(sizeof(fd_station_dev) % 4 == 0, "record size");
+    const unsigned *s = reinterpret_cast<const unsigned *>(src);
+    unsigned *d = reinterpret_cast<unsigned *>(&dst);
+    for (int k = threadIdx.x; k < (int)(sizeof(fd_station_dev) / 4); k += blockDim.x) d[k] = __ldcv(s + k);
+}
+
+__device__ __forceinline__ unsigned long long ld_acquire_sys(const unsigned long long *p)
+{
+    unsigned long long v;
+    asm volatile("ld.acquire.sys.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_release_sys(unsigned long long *p, unsigned long long v)
+{
+    asm volatile("st.release.sys.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+/* Thread 0 claims the next published request of a serving session: its entry, or -1 when the host
+ * has asked idle CTAs to stop, or -2 after q.idle_ns with nothing to claim (the host normally
+ * stops the grid long before; the bound only ends a loop whose host has gone away). */
+__device__ int serve_claim(const fd_serve_queue &q, unsigned long long *gen)
+{
+    unsigned long long t0, now;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+    for (;;) {
+        const unsigned long long h = atomicAdd(q.head, 0ull);
+        const unsigned long long t = ld_acquire_sys(q.tail);
+        if (h < t) {
+            if (atomicCAS(q.head, h, h + 1) == h) {
+                const int e = *(volatile const int *)(q.order + (h % (unsigned long long)q.ring));
+                *gen = *(volatile const unsigned long long *)(q.gen + e);
+                return e;
+            }
+            continue;
+        }
+        if (*(volatile const int *)q.stop) return -1;
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
+        if ((long long)(now - t0) > q.idle_ns) return -2;
+        __nanosleep(4000);
+    }
+}
+
+/* Batch mode (q == nullptr): station blockIdx.x / csz of `stations`, one launch per batch.
+ * Serving mode: a long-running grid of one CTA per SM; each CTA solves the requests it claims from
+ * q one after another (csz 1), and writes exitf[cta_id0 + blockIdx.x] when it leaves. */
+__global__ void __launch_bounds__(FD_BLOCK, 1) fd_solve(const fd_station_dev *stations, int nst, int dag_smem_bytes,
+                                                       int csz, const fd_serve_queue *q, int cta_id0)
+{
+    __shared__ Shared sh;
+    __shared__ fd_station_dev rec;
+    __shared__ int entry;
+    __shared__ unsigned long long gen;
+    const int station = (int)blockIdx.x / csz;
+    if (!q && station >= nst) return;   /* a whole cluster: its CTAs are consecutive */
+    for (;;) {
+        if (q) {
+            if (threadIdx.x == 0) entry = serve_claim(*q, &gen);
+            __syncthreads();
+            if (entry < 0) break;
+        }
+        load_record(rec, q ? q->desc + entry : stations + station);
+        __syncthreads();
+        solve_station(rec, dag_smem_bytes, q ? 1 : csz, sh);
+        if (!q) return;
+        /* every thread's field writes, then the statistics, then the flag the host waits for */
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence_system();
+            st_release_sys(q->done + entry, gen);
+        }
+    }
+    if (threadIdx.x == 0) {
+        __threadfence_system();
+        *(volatile int *)(q->exitf + cta_id0 + blockIdx.x) = 1;
+    }
+}
+
 }  // namespace fdk
 
 /* launch wrappers used by the host runtime */
@@ -1938,6 +2020,19 @@ extern "C" cudaError_t fdk_launch_geo_build(int nx, int ny, int nz, double h, do
 {
     fdk::fd_geo_build<<<152, 256, 0, stream>>>(nx, ny, nz, h, dq, df, z0r, ysin, zrow, node, cell);
     return cudaGetLastError();
+}
+
+/* shared memory per CTA that the dynamic part must leave: fd_solve's static shared memory, rounded
+ * up to 1 KB */
+static size_t dyn_smem_limit_margin()
+{
+    static size_t margin = 0;
+    if (!margin) {
+        cudaFuncAttributes a;
+        margin = cudaFuncGetAttributes(&a, fdk::fd_solve) == cudaSuccess ? ((a.sharedSizeBytes + 1023) & ~(size_t)1023)
+                                                                          : 4096;
+    }
+    return margin;
 }
 
 /* cluster: CTAs per station; 0 picks more than one when the stations alone would leave SMs idle,
@@ -1953,11 +2048,14 @@ extern "C" cudaError_t fdk_launch_solve(const fd_station_dev *stations, int nst,
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const long long room = optin - (long long)dyn_smem_limit_margin();
     const long long base = (long long)fdk::kSmemBase;
     const long long graph = (long long)sizeof(fdk::GraphSmem);
     const long long dagb = 2 * max_face_pad > graph ? 2 * max_face_pad : graph;
-    const long long bytes = base + dagb <= optin - 1024 ? base + dagb : (base + graph <= optin - 1024 ? base + graph : base);
-    cudaError_t e = cudaFuncSetAttribute(fdk::fd_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    const long long bytes = base + dagb <= room ? base + dagb : (base + graph <= room ? base + graph : base);
+    /* the attribute is an upper bound shared by every launch of the kernel (a serving session may
+     * launch it from another thread): always the largest */
+    cudaError_t e = cudaFuncSetAttribute(fdk::fd_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)room);
     if (e != cudaSuccess) return e;
     /* CTAs per station: with clusters of 2 any two SMs of a GPC serve; clusters of 4 and 8 are taken
      * only with room to spare, so that every cluster of the launch is co-resident (launches whose
@@ -1975,7 +2073,7 @@ extern "C" cudaError_t fdk_launch_solve(const fd_station_dev *stations, int nst,
     if (cs > FD_MAX_CLUSTER) cs = FD_MAX_CLUSTER;
     if (bytes - base < graph) cs = 1;   /* no room for the sweep-graph tables: face walks, one CTA */
     if (cs == 1) {
-        fdk::fd_solve<<<nst, FD_BLOCK, (size_t)bytes, stream>>>(stations, nst, (int)(bytes - base), 1);
+        fdk::fd_solve<<<nst, FD_BLOCK, (size_t)bytes, stream>>>(stations, nst, (int)(bytes - base), 1, nullptr, 0);
         return cudaGetLastError();
     }
     cudaLaunchConfig_t cfg = {};
@@ -1990,8 +2088,37 @@ extern "C" cudaError_t fdk_launch_solve(const fd_station_dev *stations, int nst,
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    e = cudaLaunchKernelEx(&cfg, fdk::fd_solve, stations, nst, (int)(bytes - base), cs);
+    e = cudaLaunchKernelEx(&cfg, fdk::fd_solve, stations, nst, (int)(bytes - base), cs,
+                           static_cast<const fd_serve_queue *>(nullptr), 0);
     return e == cudaSuccess ? cudaGetLastError() : e;
+}
+
+/* The long-running grid of a serving session: nctas CTAs (one per SM), numbered cta_id0 onward in
+ * q->exitf, with the largest dynamic shared memory a CTA can have (every request then finds the
+ * sweep-graph tables and, when they fit, its face's dependency bytes in shared memory). */
+extern "C" cudaError_t fdk_launch_serve(const fd_serve_queue *q, int nctas, int cta_id0, cudaStream_t stream)
+{
+    if (nctas <= 0) return cudaSuccess;
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    const long long bytes = optin - (long long)dyn_smem_limit_margin();
+    const long long base = (long long)fdk::kSmemBase;
+    if (bytes - base < (long long)sizeof(fdk::GraphSmem)) return cudaErrorInvalidConfiguration;
+    /* the same bound as every other launch of the kernel */
+    cudaError_t e = cudaFuncSetAttribute(fdk::fd_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e != cudaSuccess) return e;
+    fdk::fd_solve<<<nctas, FD_BLOCK, (size_t)bytes, stream>>>(nullptr, 0, (int)(bytes - base), 1, q, cta_id0);
+    return cudaGetLastError();
+}
+
+/* dynamic shared memory a launch of fd_solve needs in the serving loop */
+extern "C" long long fdk_serve_smem_bytes(void)
+{
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    return optin - (long long)dyn_smem_limit_margin();
 }
 
 /* slowness = 1/velocity, float division as the reference does it (src/sphfd.c:689-690) */

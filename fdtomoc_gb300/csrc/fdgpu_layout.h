@@ -134,4 +134,29 @@ typedef struct {
     fd_station_stats *stats;
 } fd_station_dev;
 
+/* Request loop of a serving session.  The host publishes station records; each CTA of the
+ * long-running solver grid claims the next one, solves it and flags it done, until the host asks
+ * idle CTAs to leave.  The host-side arrays are pinned and mapped (the CTAs read and write them
+ * across the host link); only the claim counter lives in device memory.
+ *   desc[e], gen[e]  entry e's station record and the generation (request number + 1) it holds;
+ *   order[k % ring]  the entry of the k-th published request;
+ *   tail             requests published (the host raises it after writing desc, gen and order);
+ *   head             requests claimed (device; a CTA claims k by moving head from k to k + 1);
+ *   done[e]          set to gen[e] once entry e's solve has finished and its field is written;
+ *   exitf[c]         1 once CTA c (cta_id0 + blockIdx.x) has left the loop;
+ *   stop             non-zero: a CTA with nothing to claim leaves. */
+typedef struct {
+    const fd_station_dev *desc;
+    const unsigned long long *gen;
+    const int *order;
+    const unsigned long long *tail;
+    unsigned long long *head;
+    unsigned long long *done;
+    int *exitf;
+    const int *stop;
+    int ring;
+    int pad;
+    long long idle_ns;         /* a CTA with nothing to claim for this long leaves on its own */
+} fd_serve_queue;
+
 #endif

@@ -34,6 +34,7 @@
 #include <mutex>
 
 #include "fdgpu_layout.h"
+#include "fdgpu_station.h"
 
 extern "C" cudaError_t fdk_launch_geo_build(int nx, int ny, int nz, double h, double dq, double df, double z0r,
                                             const double *ysin, double *zrow, double *node, double *cell,
@@ -64,41 +65,34 @@ int scratch_address(int dev, unsigned char **out)
     return FDGPU_OK;
 }
 
-size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+using fdh::align256;
 
-/* same checks as the allocating entry points (src/sphfd.c:533-538 for the source) */
+/* the checks of the allocating entry points, and point sources only (no starting field is
+ * supplied) */
 int check(const fdgpu_station &s)
 {
-    if (s.nx < 2 || s.ny < 2 || s.nz < 2 || !(s.h > 0) || !(s.dq != 0) || !(s.df != 0)) return FDGPU_EINVAL;
-    if (s.srctype != 1) return FDGPU_EINVAL;   /* point sources only: no starting field is supplied */
-    if (s.xs < 0 || s.ys < 0 || s.zs < 0 || s.xs > s.nx - 1 || s.ys > s.ny - 1 || s.zs > s.nz - 1)
-        return FDGPU_ESOURCE;
-    if (s.ncube < 0 || s.ncube > 64) return FDGPU_EINVAL;
-    return FDGPU_OK;
+    const int rc = fdh::check_station(s);
+    if (rc) return rc;
+    return s.srctype == 1 ? FDGPU_OK : FDGPU_EINVAL;
 }
 
 struct Plan {
-    size_t station, stats, trig, ysin, zrow, node, cell, face, end;
+    size_t station, stats, trig, ysin, face, end;
     long long max_face, max_face_pad;
 };
 
 Plan plan(const fdgpu_station &s)
 {
     Plan p;
-    const long long mf = std::max({(long long)s.nx * s.ny, (long long)s.nx * s.nz, (long long)s.ny * s.nz});
-    const int w = 2 * s.ncube + 1;
     size_t o = 0;
     p.station = o; o += align256(sizeof(fd_station_dev));
     p.stats = o;   o += align256(sizeof(fd_station_stats));
-    p.trig = o;    o += align256(sizeof(double) * 4 * (size_t)w);
-    p.ysin = o;    o += align256(sizeof(double) * (size_t)s.ny);
-    p.zrow = o;    o += align256(sizeof(double) * FD_Z_N * (size_t)s.nz);
-    p.node = o;    o += align256(sizeof(double) * FD_N_N * (size_t)s.nz * s.ny);
-    p.cell = o;    o += align256(sizeof(double) * FD_C_N * (size_t)(s.nz - 1) * (s.ny - 1));
-    p.face = o;    o += align256((size_t)(mf + 16) * 34);
+    p.trig = o;    o += align256(sizeof(double) * (size_t)fdh::box_trig_count(s));
+    p.ysin = o;    o += fdh::geo_bytes(s.ny, s.nz);   /* ysin | zrow | node | cell */
+    p.face = o;    o += fdh::face_bytes(s);
     p.end = o;
-    p.max_face = mf;
-    p.max_face_pad = (mf + 15) & ~15LL;
+    p.max_face = fdh::max_face(s);
+    p.max_face_pad = (p.max_face + 15) & ~15LL;
     return p;
 }
 
@@ -124,83 +118,26 @@ extern "C" int fdgpu_solve_noalloc(const fdgpu_station *st, const float *d_slown
 
     /* sin(colatitude) of every row, evaluated by the C library as the reference does; staged
      * through a small stack buffer (pageable copies return once the buffer may be reused) */
+    const fdh::GeoPtrs g = fdh::geo_carve(reinterpret_cast<char *>(base + p.ysin), s.ny, s.nz);
     double buf[256];
     for (int y0 = 0; y0 < s.ny; y0 += 256) {
         const int n = std::min(256, s.ny - y0);
-        for (int k = 0; k < n; k++) buf[k] = std::sin(s.y0 + s.dq * (double)(y0 + k));
-        if (cudaMemcpyAsync(base + p.ysin + sizeof(double) * y0, buf, sizeof(double) * n, cudaMemcpyHostToDevice,
-                            cs) != cudaSuccess)
+        for (int k = 0; k < n; k++) buf[k] = std::sin(fdh::qc(s, y0 + k));
+        if (cudaMemcpyAsync(g.ysin + y0, buf, sizeof(double) * n, cudaMemcpyHostToDevice, cs) != cudaSuccess)
             return FDGPU_ECUDA;
     }
-    double *ysin = reinterpret_cast<double *>(base + p.ysin);
-    double *zrow = reinterpret_cast<double *>(base + p.zrow);
-    double *node = reinterpret_cast<double *>(base + p.node);
-    double *cell = reinterpret_cast<double *>(base + p.cell);
-    if (fdk_launch_geo_build(s.nx, s.ny, s.nz, s.h, s.dq, s.df, s.z0r, ysin, zrow, node, cell, cs) != cudaSuccess)
+    if (fdk_launch_geo_build(s.nx, s.ny, s.nz, s.h, s.dq, s.df, s.z0r, g.ysin, g.zrow, g.node, g.cell, cs)
+        != cudaSuccess)
         return FDGPU_ECUDA;
 
-    /* the station descriptor, as the allocating path builds it */
+    /* the station descriptor, as the allocating path builds it, without sweep-graph arrays */
     fd_station_dev d;
-    std::memset(&d, 0, sizeof d);
-    d.g.nx = s.nx; d.g.ny = s.ny; d.g.nz = s.nz;
-    d.g.h = s.h; d.g.inv_h = 1.0 / s.h; d.g.dq = s.dq; d.g.df = s.df; d.g.is_h = 1.0 / (s.h * s.h);
-    d.g.zrow = zrow; d.g.ysin = ysin; d.g.node = node; d.g.cell = cell;
-    d.T = d_time;
-    d.S = d_slowness + (long long)s.oz * s_sz + (long long)s.oy * s_sy + s.ox;
-    d.s_sy = s_sy; d.s_sz = s_sz;
-    /* initial box of the point source (src/sphfd.c:766-825), walls in face order z1 z2 x2 x1 y1 y2 */
-    const int nc = s.ncube;
-    for (int f = 0; f < 6; f++) d.dflag[f] = 1;
-    if (s.xs > nc) d.wall[3] = s.xs - (nc + 1); else { d.wall[3] = -1; d.dflag[3] = 0; }
-    if (s.xs < s.nx - (nc + 1)) d.wall[2] = s.xs + (nc + 1); else { d.wall[2] = s.nx; d.dflag[2] = 0; }
-    if (s.ys > nc) d.wall[4] = s.ys - (nc + 1); else { d.wall[4] = -1; d.dflag[4] = 0; }
-    if (s.ys < s.ny - (nc + 1)) d.wall[5] = s.ys + (nc + 1); else { d.wall[5] = s.ny; d.dflag[5] = 0; }
-    if (s.zs > nc) d.wall[0] = s.zs - (nc + 1); else { d.wall[0] = -1; d.dflag[0] = 0; }
-    if (s.zs < s.nz - (nc + 1)) d.wall[1] = s.zs + (nc + 1); else { d.wall[1] = s.nz; d.dflag[1] = 0; }
-    const int grow[6] = {s.kminus, s.kplus, s.iplus, s.iminus, s.jminus, s.jplus};
-    for (int f = 0; f < 6; f++) d.grow[f] = grow[f];
-    d.radius = nc;
-    d.reverse = s.reverse;
-    /* preferred restart wall (src/sphfd.c:977-1003) */
-    int hp = s.headpref;
-    if (hp > 0) {
-        const int x1 = d.wall[3], x2 = d.wall[2], y1 = d.wall[4], y2 = d.wall[5], z1 = d.wall[0], z2 = d.wall[1];
-        long long head = (long long)s.nx * s.ny * s.nz;
-        if (s.nx > 5 && x2 <= head) { hp = 2; head = x2; }
-        if (s.nx > 5 && (s.nx - 1 - x1) <= head) { hp = 1; head = s.nx - 1 - x1; }
-        if (s.ny > 5 && y2 <= head) { hp = 4; head = y2; }
-        if (s.ny > 5 && (s.ny - 1 - y1) <= head) { hp = 3; head = s.ny - 1 - y1; }
-        if (s.nz > 5 && z2 <= head) { hp = 6; head = z2; }
-        if (s.nz > 5 && (s.nz - 1 - z1) <= head) { hp = 5; head = s.nz - 1 - z1; }
-    }
-    d.headpref = hp;
-    d.maxrad = s.maxrad;
-    d.init_mode = 0;
-    d.xs = s.xs; d.ys = s.ys; d.zs = s.zs; d.ncube = nc;
-    const double fxss = s.src_geo[0], fyss = s.src_geo[1], fzss = s.src_geo[2];
-    d.src_xyz[0] = fzss * std::cos(fyss);
-    d.src_xyz[1] = fzss * std::sin(fyss) * std::cos(fxss);
-    d.src_xyz[2] = fzss * std::sin(fyss) * std::sin(fxss);
-    const int w = 2 * nc + 1;
+    fdh::fill_station(d, s, g, d_time, d_slowness, s_sy, s_sz, 0, reinterpret_cast<char *>(base + p.face), nullptr,
+                      reinterpret_cast<const double *>(base + p.trig),
+                      reinterpret_cast<fd_station_stats *>(base + p.stats));
+    const int w = 2 * s.ncube + 1;
     double trig[4 * 129];
-    for (int j = 0; j < w; j++) {
-        const double q = s.y0 + s.dq * (double)(s.ys - nc + j), f = s.x0 + s.df * (double)(s.xs - nc + j);
-        trig[2 * j] = std::cos(q);
-        trig[2 * j + 1] = std::sin(q);
-        trig[2 * w + 2 * j] = std::cos(f);
-        trig[2 * w + 2 * j + 1] = std::sin(f);
-    }
-    d.box_trig = reinterpret_cast<const double *>(base + p.trig);
-    const size_t m = (size_t)p.max_face;
-    unsigned char *fb = base + p.face;
-    d.scr.key = reinterpret_cast<unsigned long long *>(fb);
-    d.scr.rec = reinterpret_cast<float2 *>(fb + 8 * m);
-    d.scr.pst = reinterpret_cast<int *>(fb + 16 * m);
-    d.scr.queue = reinterpret_cast<int *>(fb + 20 * m);
-    d.scr.rq = reinterpret_cast<int *>(fb + 24 * m);
-    d.scr.dag = fb + 32 * m;
-    d.max_face_pad = p.max_face_pad;
-    d.stats = reinterpret_cast<fd_station_stats *>(base + p.stats);
+    fdh::box_trig(s, trig);
 
     if (cudaMemcpyAsync(base + p.trig, trig, sizeof(double) * 4 * (size_t)w, cudaMemcpyHostToDevice, cs) != cudaSuccess
         || cudaMemsetAsync(base + p.stats, 0, sizeof(fd_station_stats), cs) != cudaSuccess
@@ -213,20 +150,6 @@ extern "C" int fdgpu_solve_noalloc(const fdgpu_station *st, const float *d_slown
     if (cudaMemcpyAsync(&hs, base + p.stats, sizeof hs, cudaMemcpyDeviceToHost, cs) != cudaSuccess
         || cudaStreamSynchronize(cs) != cudaSuccess)
         return FDGPU_ECUDA;
-    if (stats) {
-        std::memset(stats, 0, sizeof *stats);
-        stats->status = hs.status ? FDGPU_ESCHED : FDGPU_OK;
-        stats->sweeps = hs.sweeps;
-        stats->node_updates = hs.node_updates;
-        stats->faces = hs.faces;
-        stats->rounds = hs.rounds;
-        stats->deferred = hs.deferred;
-        for (int j = 0; j < 5; j++) stats->stencils[j] = hs.stencils[j];
-        for (int j = 0; j < 8; j++) stats->restart_wall[j] = hs.restart_wall[j];
-        stats->t_start_ns = hs.t_start_ns;
-        stats->t_end_ns = hs.t_end_ns;
-        stats->pipelined_sweeps = hs.pipelined_sweeps;
-        stats->detail = hs.status;
-    }
+    if (stats) fdh::copy_stats(*stats, hs);
     return hs.status ? FDGPU_ESCHED : FDGPU_OK;
 }

@@ -49,6 +49,42 @@ class Stats(C.Structure):
                     detail=self.detail)
 
 
+class ServeOpts(C.Structure):
+    """fdgpu_serve_opts."""
+
+    _fields_ = [("hbm_bytes", C.c_longlong), ("max_inflight", C.c_int), ("reserve_sms", C.c_int),
+                ("max_models", C.c_int), ("idle_stop_us", C.c_int)]
+
+
+class ServeResult(C.Structure):
+    """fdgpu_serve_result."""
+
+    _fields_ = [("id", C.c_uint64), ("tag", C.c_uint64), ("status", C.c_int32), ("model_version", C.c_int32),
+                ("queue_ms", C.c_double), ("latency_ms", C.c_double), ("solve_ms", C.c_double), ("stats", Stats)]
+
+    def as_dict(self):
+        return dict(id=self.id, tag=self.tag, status=self.status, model_version=self.model_version,
+                    queue_ms=self.queue_ms, latency_ms=self.latency_ms, solve_ms=self.solve_ms,
+                    stats=self.stats.as_dict())
+
+
+class ServeMetrics(C.Structure):
+    """fdgpu_serve_metrics."""
+
+    _fields_ = [("submitted", C.c_int64), ("completed", C.c_int64), ("failed", C.c_int64), ("queued", C.c_int64),
+                ("inflight", C.c_int64), ("p50_ms", C.c_double), ("p90_ms", C.c_double), ("p99_ms", C.c_double),
+                ("max_ms", C.c_double), ("mean_ms", C.c_double), ("solve_p50_ms", C.c_double),
+                ("solve_p99_ms", C.c_double), ("fields_per_s", C.c_double), ("node_updates_per_s", C.c_double),
+                ("node_updates", C.c_int64), ("hbm_bytes", C.c_int64), ("hbm_used", C.c_int64),
+                ("hbm_peak", C.c_int64), ("solver_ctas", C.c_int32), ("grid_launches", C.c_int32),
+                ("hist", C.c_int64 * 40)]
+
+    def as_dict(self):
+        d = {name: getattr(self, name) for name, _ in self._fields_ if name != "hist"}
+        d["hist"] = list(self.hist)
+        return d
+
+
 class FdgpuError(RuntimeError):
     pass
 
@@ -82,6 +118,17 @@ def load() -> C.CDLL:
         lib.fdgpu_velocity_to_slowness.argtypes = [P, C.c_void_p, C.c_void_p, C.c_longlong, C.c_void_p]
         lib.fdgpu_sphfd.argtypes = [C.c_int, C.POINTER(C.c_char_p), C.c_char_p]
         lib.fdgpu_sphfd_parlist.argtypes = [C.c_int, C.POINTER(C.c_char_p), C.c_char_p, C.POINTER(C.c_int)]
+        lib.fdgpu_serve_open.argtypes = [C.c_int, C.POINTER(ServeOpts), C.POINTER(P)]
+        lib.fdgpu_serve_set_model.argtypes = [P, C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_int,
+                                              C.POINTER(C.c_int)]
+        lib.fdgpu_serve_submit.argtypes = [P, C.POINTER(Station), C.c_int, C.c_void_p, C.c_void_p, C.c_uint64,
+                                           C.POINTER(C.c_uint64)]
+        lib.fdgpu_serve_poll.argtypes = [P, C.POINTER(ServeResult), C.c_int, C.c_int, C.POINTER(C.c_int)]
+        lib.fdgpu_serve_drain.argtypes = [P, C.c_int]
+        lib.fdgpu_serve_metrics_get.argtypes = [P, C.POINTER(ServeMetrics)]
+        lib.fdgpu_serve_last_error.argtypes = [P]
+        lib.fdgpu_serve_last_error.restype = C.c_char_p
+        lib.fdgpu_serve_close.argtypes = [P]
         _lib = lib
     return _lib
 
@@ -187,3 +234,85 @@ def sphfd_parlist(entries, timedir: str):
     status = (C.c_int * n)()
     lib.fdgpu_sphfd_parlist(n, argv, timedir.encode(), status)
     return list(status)
+
+
+def _addr(buf) -> int:
+    """Address of a numpy array or of a tensor-like object with data_ptr()."""
+    if isinstance(buf, np.ndarray):
+        if not buf.flags.c_contiguous or buf.dtype != np.float32:
+            raise FdgpuError("buffers must be C-contiguous float32")
+        return buf.ctypes.data
+    return int(buf.data_ptr())
+
+
+class Server:
+    """A serving session (fdgpu_serve_*): device-resident models, requests solved as they arrive by
+    a long-running grid of solver CTAs.  Buffers passed to submit() are kept referenced until their
+    result has been polled."""
+
+    def __init__(self, device: int = 0, hbm_bytes: int = 0, max_inflight: int = 0, reserve_sms: int = -1,
+                 max_models: int = 2, idle_stop_us: int = 0):
+        self.lib = load()
+        self.ptr = C.c_void_p()
+        opts = ServeOpts(hbm_bytes, max_inflight, reserve_sms, max_models, idle_stop_us)
+        _check(self.lib.fdgpu_serve_open(device, C.byref(opts), C.byref(self.ptr)))
+        self._keep = {}
+
+    def _check(self, rc):
+        if rc != FDGPU_OK:
+            extra = self.lib.fdgpu_serve_last_error(self.ptr).decode() if self.ptr else ""
+            msg = self.lib.fdgpu_strerror(rc).decode() + (": " + extra if extra else "")
+            raise FdgpuError(f"fdgpu error {rc} ({ERRORS.get(rc, '?')}): {msg}")
+
+    def set_model(self, model: int, velocity) -> int:
+        """velocity: (nz, ny, nx) float32, a numpy array or a device tensor.  Returns the version."""
+        mnz, mny, mnx = velocity.shape
+        ver = C.c_int()
+        self._check(self.lib.fdgpu_serve_set_model(self.ptr, model, C.c_void_p(_addr(velocity)), mnx, mny, mnz,
+                                                   C.byref(ver)))
+        return ver.value
+
+    def submit(self, station: Station, model: int, out, init=None, tag: int = 0) -> int:
+        """Queue a solve; out (nz, ny, nx) float32 receives the field (host array or device tensor)."""
+        rid = C.c_uint64()
+        ip = C.c_void_p(_addr(init)) if init is not None else None
+        self._check(self.lib.fdgpu_serve_submit(self.ptr, C.byref(station), model, C.c_void_p(_addr(out)), ip, tag,
+                                                C.byref(rid)))
+        self._keep[rid.value] = (out, init)
+        return rid.value
+
+    def poll(self, max_results: int = 256, timeout_ms: int = 0):
+        buf = (ServeResult * max_results)()
+        n = C.c_int()
+        self._check(self.lib.fdgpu_serve_poll(self.ptr, buf, max_results, timeout_ms, C.byref(n)))
+        out = [buf[k].as_dict() for k in range(n.value)]
+        for r in out:
+            self._keep.pop(r["id"], None)
+        return out
+
+    def drain(self, timeout_ms: int = -1):
+        self._check(self.lib.fdgpu_serve_drain(self.ptr, timeout_ms))
+
+    def metrics(self) -> dict:
+        m = ServeMetrics()
+        self._check(self.lib.fdgpu_serve_metrics_get(self.ptr, C.byref(m)))
+        return m.as_dict()
+
+    def close(self):
+        if self.ptr:
+            rc = self.lib.fdgpu_serve_close(self.ptr)
+            self.ptr = C.c_void_p()
+            self._keep.clear()
+            _check(rc)
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

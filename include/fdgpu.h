@@ -10,8 +10,10 @@
  *                                       (src/sphfd.c:194, body :260-5803)
  *        fdgpu_sphfd_parlist  replaces  the OpenMP loop over par files in main()
  *                                       (src/sphfd.c:247-255); all stations run on the GPU at once.
- *   2. Array entry points for callers that keep models and fields in memory (the batch and
- *      serving drivers): fdgpu_station_from_par, fdgpu_solve_host, fdgpu_solve_device.
+ *   2. Array entry points for callers that keep models and fields in memory (batch drivers):
+ *      fdgpu_station_from_par, fdgpu_solve_host, fdgpu_solve_device, fdgpu_solve_noalloc.
+ *   3. A serving session (fdgpu_serve_*): models resident on the device, requests admitted as
+ *      they arrive and solved by a long-running grid, with latency statistics.
  *
  * Conventions: every function returns an FDGPU_* status (0 = success) and never aborts; the
  * caller owns host buffers and any device buffers it passes in; the library owns its scratch,
@@ -38,7 +40,8 @@ enum {
     FDGPU_ESOURCE = -6,  /* the source is outside the grid (src/sphfd.c:533-538) */
     FDGPU_ESCHED = -7,   /* internal: a walk's schedule check failed (fdgpu_stats.detail says which) */
     FDGPU_ENODEV = -8,   /* no CUDA device */
-    FDGPU_ETOOBIG = -9   /* the problem needs more than fdgpu_solve_noalloc's static scratch */
+    FDGPU_ETOOBIG = -9   /* the problem needs more memory than the entry point may use
+                            (fdgpu_solve_noalloc's static scratch, a serving session's memory) */
 };
 
 typedef struct fdgpu_ctx fdgpu_ctx;
@@ -141,6 +144,99 @@ int fdgpu_probe_fp64(fdgpu_ctx *ctx, double *gops);
 #define FDGPU_NOALLOC_SCRATCH_BYTES (16u << 20)
 int fdgpu_solve_noalloc(const fdgpu_station *st, const float *d_slowness, long long s_sy, long long s_sz,
                         float *d_time, fdgpu_stats *stats, void *stream);
+
+/* ---- Serving -------------------------------------------------------------------------------
+ *
+ * A serving session keeps velocity models on the device and solves station requests as they
+ * arrive.  It has no counterpart in the reference, whose driver runs one sphfd() per par file
+ * under OpenMP (src/sphfd.c:247-255) and reads the model from disk in every call (:586-700).
+ *
+ * One long-running grid of solver CTAs (one per SM, less reserve_sms) loops on the device: each
+ * CTA claims the next published request, solves it and flags it done.  A host thread admits
+ * requests in submission order whenever a request slot and enough of the session's device memory
+ * are free (the field, the solve's scratch and the geometry tables it needs), publishes them to the
+ * grid, copies finished fields to host buffers, and records latencies.  Requests that arrive while
+ * others run are therefore solved alongside them, and a result does not depend on what else is in
+ * flight: it is bit-identical to fdgpu_solve_device of the same station.  The grid leaves the GPU
+ * after idle_stop_us with nothing in flight and comes back with the next request.
+ *
+ * All functions may be called from any host thread. */
+typedef struct fdgpu_server fdgpu_server;
+
+typedef struct {
+    long long hbm_bytes;   /* device memory the session holds for models, geometry tables and the
+                              working sets of admitted solves; 0: half the free memory at open */
+    int max_inflight;      /* requests admitted at once (published, running or being copied out);
+                              0: twice the number of solver CTAs */
+    int reserve_sms;       /* SMs left without a solver CTA, for the session's own small kernels and
+                              for other work; at least 1; -1: 2 */
+    int max_models;        /* model slots, e.g. 2 for P and S; 0: 2 */
+    int idle_stop_us;      /* the grid leaves after this long with nothing in flight; 0: 2000 */
+} fdgpu_serve_opts;
+
+typedef struct {
+    uint64_t id;           /* as returned by fdgpu_serve_submit */
+    uint64_t tag;          /* the caller's tag */
+    int32_t status;        /* FDGPU_OK or the failure */
+    int32_t model_version; /* version of the model slot the request was solved against */
+    double queue_ms;       /* submission to publication on the device */
+    double latency_ms;     /* submission to the field being in the caller's buffer */
+    double solve_ms;       /* the solve on its CTA (GPU timer) */
+    fdgpu_stats stats;
+} fdgpu_serve_result;
+
+typedef struct {
+    int64_t submitted, completed, failed;
+    int64_t queued;          /* submitted, not yet admitted */
+    int64_t inflight;        /* admitted, not yet completed */
+    double p50_ms, p90_ms, p99_ms, max_ms, mean_ms;   /* latency of completed requests */
+    double solve_p50_ms, solve_p99_ms;                /* GPU solve time of completed requests */
+    double fields_per_s;     /* completed / (last completion - first submission) */
+    double node_updates_per_s;
+    int64_t node_updates;
+    int64_t hbm_bytes;       /* session memory */
+    int64_t hbm_used, hbm_peak;   /* held now, largest held */
+    int32_t solver_ctas;     /* CTAs of the solver grid */
+    int32_t grid_launches;   /* times the grid was launched */
+    int64_t hist[40];        /* latency histogram: hist[k] counts latencies in [2^(k-10), 2^(k-9)) ms
+                                (the first and last buckets are open-ended) */
+} fdgpu_serve_metrics;
+
+int fdgpu_serve_open(int device, const fdgpu_serve_opts *opts, fdgpu_server **out);
+
+/* Set model slot `model` to a velocity model (mnx, mny, mnz floats, x fastest; host or device
+ * memory).  It is converted to slowness on the device as the reference rounds it
+ * (src/sphfd.c:689).  Requests submitted afterwards use the new version; requests submitted
+ * before keep the one they were submitted against, which is freed when the last of them
+ * completes.  *version (may be NULL) receives the new version number (1, 2, ...). */
+int fdgpu_serve_set_model(fdgpu_server *sv, int model, const float *velocity, int mnx, int mny, int mnz,
+                          int *version);
+
+/* Queue one solve of station st against model slot `model` (st->ox/oy/oz place its window).
+ * times (nx*ny*nz floats) receives the field: device memory (the solve writes it in place) or host
+ * memory (pinned or not; copied when the solve is done).  It must stay valid until the request's
+ * result has been polled.  init_times (host or device, may be NULL) is the starting field of a
+ * srctype 2/3 station.  Returns at once; *id (may be NULL) receives the request id.
+ * FDGPU_ETOOBIG: the request can never fit the session's memory. */
+int fdgpu_serve_submit(fdgpu_server *sv, const fdgpu_station *st, int model, float *times, const float *init_times,
+                       uint64_t tag, uint64_t *id);
+
+/* Completed requests, in completion order: up to max results into out, *n of them.  Waits up to
+ * timeout_ms for the first one (0: do not wait; -1: until one completes or nothing is left
+ * outstanding). */
+int fdgpu_serve_poll(fdgpu_server *sv, fdgpu_serve_result *out, int max, int timeout_ms, int *n);
+
+/* Wait until every submitted request has completed (timeout_ms -1: no limit).  FDGPU_ECUDA if the
+ * limit passed first. */
+int fdgpu_serve_drain(fdgpu_server *sv, int timeout_ms);
+
+int fdgpu_serve_metrics_get(fdgpu_server *sv, fdgpu_serve_metrics *m);
+
+/* text of the session's last CUDA failure ("" if none) */
+const char *fdgpu_serve_last_error(const fdgpu_server *sv);
+
+/* Complete every outstanding request, stop the grid and free the session. */
+int fdgpu_serve_close(fdgpu_server *sv);
 
 /* Drop-in sphfd(): ac/av as the reference's (av[1] = "par=<file>"), output_path = timedir.
  * Reads the velocity file, solves on the GPU, writes <output_path>/<timefile> byte-for-byte as

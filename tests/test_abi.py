@@ -35,6 +35,17 @@ def test_no_device_is_an_error_not_a_fallback(gpu_lib):
         gpu_lib.Context(0)
 
 
+def test_serving_without_device_is_an_error(gpu_lib):
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("a GPU is present")
+    except ImportError:
+        pass
+    with pytest.raises(gpu_lib.FdgpuError, match="ENODEV"):
+        gpu_lib.Server(0)
+
+
 def test_station_from_par_matches_sphfd_setup(gpu_lib, tmp_path):
     """Geocentric set-up of src/sphfd.c:415-509 for the M001 par file."""
     from fdtomoc_gb300.formats import write_par

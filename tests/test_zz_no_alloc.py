@@ -68,4 +68,4 @@ def test_noalloc_rejects_too_large(gpu_lib, tmp_path):
     dummy = torch.zeros(16, dtype=torch.float32, device="cuda")
     rc = L.fdgpu_solve_noalloc(C.byref(big), dummy.data_ptr(), 401, 401 * 401, dummy.data_ptr(), None, None)
     assert rc == -9
-    assert b"static scratch" in lib.load().fdgpu_strerror(rc)
+    assert b"exceeds the memory" in lib.load().fdgpu_strerror(rc)
