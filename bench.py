@@ -48,6 +48,8 @@ def parse():
     ap.add_argument("--config", type=int, default=2, choices=[1, 2],
                     help="2: the benchmark workload; 1: the one-station 61x61x31 case, for profiling")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--serve-requests", type=int, default=300,
+                    help="requests of the serving leg (0: skip it)")
     args = ap.parse_args()
     if args.stations is None:
         args.stations = STATIONS_PER_GPU if args.config == 2 else 1
@@ -177,6 +179,38 @@ class ClockSampler:
 # GPU arm
 
 
+def serve_leg(args, lib, stations, v, batch_fields):
+    """Serving: P and S requests for the workload's stations (S = P/1.73 with an independent 2 %
+    perturbation), all submitted at once to a serving session that keeps both models and every
+    field on the device; throughput, latency percentiles, and the P fields checked bit for bit
+    against the batch step's."""
+    import numpy as np
+    import torch
+    from fdtomoc_gb300 import workloads as W
+    n = args.serve_requests
+    vs = (v / 1.73 * (1.0 + 0.02 * W.smooth_noise(v.shape, (0.5, 0.556, 0.509), 10.0, 44))).astype(np.float32)
+    reqs = [(stations[k // 2 % len(stations)], k % 2) for k in range(n)]
+    outs = [torch.empty(st.shape, dtype=torch.float32, device="cuda") for st, _ in reqs]
+    torch.cuda.synchronize()
+    with lib.Server(torch.cuda.current_device(), hbm_bytes=min(96 << 30, (8 << 30) + n * (96 << 20))) as sv:
+        sv.set_model(0, v)
+        sv.set_model(1, vs)
+        t0 = time.time()
+        for k, (st, phase) in enumerate(reqs):
+            sv.submit(st, phase, outs[k], tag=k)
+        sv.drain(1800000)
+        wall = time.time() - t0
+        res = sv.poll(n + 8)
+        m = sv.metrics()
+    bad = sum(1 for r in res if r["status"] != 0)
+    same = all(torch.equal(outs[2 * k], batch_fields[k]) for k in range(min(len(batch_fields), n // 2)))
+    return {"requests": n, "phases": "P and S alternating", "fields_per_s": n / wall, "wall_s": wall,
+            "node_updates_per_s": m["node_updates"] / wall, "latency_ms": {"p50": m["p50_ms"], "p99": m["p99_ms"]},
+            "solve_ms": {"p50": m["solve_p50_ms"], "p99": m["solve_p99_ms"]}, "solver_ctas": m["solver_ctas"],
+            "hbm_peak_bytes": m["hbm_peak"], "failed": bad, "p_fields_equal_batch": same,
+            "what": "all requests submitted at once; latency = submission to field ready on the device"}
+
+
 def run_gpu(args):
     rank, world, local = dist_env()
     n = args.stations
@@ -299,6 +333,8 @@ def run_gpu(args):
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         e2e["value"] = total_stations / float(t.item())
 
+    serving = serve_leg(args, lib, stations, v, fields) if args.serve_requests > 0 else None
+
     # roofline of the solve kernel (one launch per step): algorithmic bytes 12 B per node update
     peaks = {}
     try:
@@ -341,6 +377,8 @@ def run_gpu(args):
             "clocks": clocks,
             "sweeps": [s["sweeps"] for s in all_stats[-1]][:8],
         }
+        if serving is not None:
+            line["serving"] = serving
         if cpu is not None:
             line["cpu_baseline"] = cpu
         print(json.dumps(line), flush=True)

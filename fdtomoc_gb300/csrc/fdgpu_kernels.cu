@@ -1923,6 +1923,9 @@ __device__ __forceinline__ void solve_station(const fd_station_dev &sd, int dag_
         o->t_start_ns = (int64_t)t_start;
         o->t_end_ns = (int64_t)t_end;
         o->pipelined_sweeps = (int32_t)sh.gsweeps;
+        unsigned smid;
+        asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
+        o->sm = (int32_t)smid;
     }
     /* no CTA leaves while another may still read the first CTA's shared memory; every wait before
      * this line is bounded, so every CTA reaches it */
@@ -1958,8 +1961,9 @@ __device__ int serve_claim(const fd_serve_queue &q, unsigned long long *gen)
 {
     unsigned long long t0, now;
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+    unsigned sleep_ns = 500;
     for (;;) {
-        const unsigned long long h = atomicAdd(q.head, 0ull);
+        const unsigned long long h = *(volatile const unsigned long long *)q.head;
         const unsigned long long t = ld_acquire_sys(q.tail);
         if (h < t) {
             if (atomicCAS(q.head, h, h + 1) == h) {
@@ -1972,7 +1976,10 @@ __device__ int serve_claim(const fd_serve_queue &q, unsigned long long *gen)
         if (*(volatile const int *)q.stop) return -1;
         asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
         if ((long long)(now - t0) > q.idle_ns) return -2;
-        __nanosleep(4000);
+        /* idle CTAs back off to one look every ~0.2 ms: a claim waits at most that long, and the
+         * CTAs that are solving share the memory system with fewer polls */
+        __nanosleep(sleep_ns);
+        if (sleep_ns < 200000) sleep_ns *= 2;
     }
 }
 

@@ -72,7 +72,7 @@ typedef struct {
                                 set-up, phases A, B, C and the face walks (zero otherwise) */
     int64_t t_start_ns, t_end_ns; /* GPU global timer when the station's solve began and ended */
     int32_t pipelined_sweeps;
-    int32_t pad;
+    int32_t sm;              /* the SM whose CTA ran the solve */
 } fd_station_stats;
 
 /* One face instance of a sweep graph: a face walked at one wall position, with its point

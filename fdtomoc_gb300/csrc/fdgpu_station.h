@@ -231,6 +231,7 @@ inline void copy_stats(fdgpu_stats &o, const fd_station_stats &h)
     o.t_start_ns = h.t_start_ns;
     o.t_end_ns = h.t_end_ns;
     o.pipelined_sweeps = h.pipelined_sweeps;
+    o.sm = h.sm;
     o.detail = h.status;
 }
 

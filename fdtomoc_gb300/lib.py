@@ -39,13 +39,14 @@ class Stats(C.Structure):
     _fields_ = [("status", C.c_int32), ("sweeps", C.c_int32), ("node_updates", C.c_int64), ("faces", C.c_int64),
                 ("rounds", C.c_int64), ("deferred", C.c_int64), ("stencils", C.c_int64 * 5),
                 ("restart_wall", C.c_int32 * 8), ("phase_cycles", C.c_int64 * 6), ("t_start_ns", C.c_int64),
-                ("t_end_ns", C.c_int64), ("pipelined_sweeps", C.c_int32), ("detail", C.c_int32)]
+                ("t_end_ns", C.c_int64), ("pipelined_sweeps", C.c_int32), ("detail", C.c_int32),
+                ("sm", C.c_int32), ("pad", C.c_int32)]
 
     def as_dict(self):
         return dict(status=self.status, sweeps=self.sweeps, node_updates=self.node_updates, faces=self.faces,
                     rounds=self.rounds, deferred=self.deferred, stencils=list(self.stencils),
                     restart_wall=list(self.restart_wall), phase_cycles=list(self.phase_cycles),
-                    t_start_ns=self.t_start_ns, t_end_ns=self.t_end_ns, pipelined_sweeps=self.pipelined_sweeps,
+                    t_start_ns=self.t_start_ns, t_end_ns=self.t_end_ns, pipelined_sweeps=self.pipelined_sweeps, sm=self.sm,
                     detail=self.detail)
 
 

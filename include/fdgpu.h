@@ -84,6 +84,8 @@ typedef struct {
                                  releases, 4 sweep bound, 6 a pipelined sweep met a point needing an
                                  earlier point's stencil state, 8 a worker waited too long, 9 a
                                  claimed queue entry was never written, 10 a node queued twice */
+    int32_t sm;               /* the SM whose CTA ran the solve */
+    int32_t pad;
 } fdgpu_stats;
 
 int fdgpu_create(int device, fdgpu_ctx **out);
