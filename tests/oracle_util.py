@@ -35,3 +35,88 @@ def run_oracle(parfile: str, timedir: str, fast: bool = False):
     if rc != 0:
         raise RuntimeError(f"oracle failed on {parfile}: {rc}")
     return st
+
+
+# ---- location oracle (oracle/fd_locate.c) ----------------------------------------------------
+
+class LocGrid(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("x0", C.c_double), ("y0", C.c_double),
+                ("z0", C.c_double), ("h", C.c_double), ("dq", C.c_double), ("df", C.c_double),
+                ("xmax", C.c_float), ("ymax", C.c_float), ("zmax", C.c_float), ("z0r", C.c_double),
+                ("kmin", C.c_int), ("ndiv", C.c_int), ("ndiv2", C.c_int), ("ivs", C.c_int), ("vpvs", C.c_float),
+                ("nthres", C.c_int), ("resthres", C.c_float), ("resthrep", C.c_float), ("stdmax", C.c_float)]
+
+
+class LocObs(C.Structure):
+    _fields_ = [("field", C.c_int), ("obstime", C.c_float), ("pwt", C.c_float), ("phase", C.c_char),
+                ("good", C.c_int)]
+
+
+class LocResult(C.Structure):
+    _fields_ = [("status", C.c_int), ("ngood", C.c_int), ("nxx", C.c_int), ("nyy", C.c_int), ("nzz", C.c_int),
+                ("passes", C.c_int), ("exm", C.c_double), ("eym", C.c_double), ("ezm", C.c_double),
+                ("stdmin", C.c_float), ("avrmin", C.c_float)]
+
+
+def loc_lib():
+    lib = load_oracle()
+    if not getattr(lib, "_loc_bound", False):
+        lib.fdo_loc_grid_from_spec.argtypes = [C.POINTER(LocGrid), C.c_int, C.c_int, C.c_int, C.c_double,
+                                               C.c_double, C.c_double, C.c_double]
+        lib.fdo_locate.argtypes = [C.POINTER(LocGrid), C.POINTER(C.POINTER(C.c_float)), C.c_int,
+                                   C.POINTER(LocObs), C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                   C.POINTER(LocResult)]
+        lib.fdo_htoe.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_double]
+        lib.fdo_htoe.restype = C.c_double
+        lib.fdo_etoh.argtypes = [C.c_double, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                 C.POINTER(C.c_int), C.POINTER(C.c_double)]
+        lib.fdo_glathinv.argtypes = [C.c_double, C.c_double, C.POINTER(C.c_double)]
+        lib.fdo_glathinv.restype = C.c_double
+        lib.fdo_loc_hpi.restype = C.c_double
+        lib.fdo_loc_degrad.restype = C.c_double
+        lib._loc_bound = True
+    return lib
+
+
+def loc_helpers(grid):
+    """htoe / etoh / glathinv of the oracle, and the grid's constants, for loc_cases.format_outputs"""
+    lib = loc_lib()
+
+    def etoh(e):
+        y, d, h, m, s = C.c_int(), C.c_int(), C.c_int(), C.c_int(), C.c_double()
+        lib.fdo_etoh(e, C.byref(y), C.byref(d), C.byref(h), C.byref(m), C.byref(s))
+        return y.value, d.value, h.value, m.value, s.value
+
+    def glathinv(x, r):
+        hh = C.c_double()
+        lat = lib.fdo_glathinv(x, r, C.byref(hh))
+        return lat, hh.value
+
+    return dict(htoe=lib.fdo_htoe, etoh=etoh, glathinv=glathinv, hpi=lib.fdo_loc_hpi(),
+                degrad=lib.fdo_loc_degrad(), z0r=grid.z0r)
+
+
+def loc_grid(p):
+    lib = loc_lib()
+    g = LocGrid()
+    lib.fdo_loc_grid_from_spec(C.byref(g), p["nx"], p["ny"], p["nz"], p["x0"], p["y0"], p["z0"], p["h"])
+    g.kmin, g.ndiv, g.ndiv2 = p["kmin"], p["ndiv"], p["ndiv2"]
+    g.nthres, g.resthres, g.resthrep, g.stdmax = p["nthres"], p["resthres"], p["resthrep"], p["stdmax"]
+    return g
+
+
+def oracle_locate(grid, field_list, obs):
+    """obs: list of (field index, obstime, pwt, phase, good); returns a result dict as
+    loc_cases.format_outputs reads it."""
+    lib = loc_lib()
+    n = len(obs)
+    arr = (LocObs * n)(*[LocObs(f, t, w, ph.encode(), g) for f, t, w, ph, g in obs])
+    fp = (C.POINTER(C.c_float) * len(field_list))(*[f.ctypes.data_as(C.POINTER(C.c_float)) for f in field_list])
+    resmin = (C.c_float * n)()
+    tps = (C.c_float * n)()
+    r = LocResult()
+    rc = lib.fdo_locate(C.byref(grid), fp, n, arr, resmin, tps, C.byref(r))
+    assert rc == 0
+    return dict(status=r.status, ngood=r.ngood, nxx=r.nxx, nyy=r.nyy, nzz=r.nzz, passes=r.passes, exm=r.exm,
+                eym=r.eym, ezm=r.ezm, stdmin=r.stdmin, avrmin=r.avrmin, good=[a.good for a in arr],
+                resmin=list(resmin), tps=list(tps))
