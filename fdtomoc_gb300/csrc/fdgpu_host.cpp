@@ -215,6 +215,14 @@ extern "C" int fdgpu_probe_fp64(fdgpu_ctx *ctx, double *gops)
     return FDGPU_OK;
 }
 
+/* context access for the library's other translation units */
+extern "C" int fdh_ctx_device(const fdgpu_ctx *ctx) { return ctx->device; }
+extern "C" void *fdh_ctx_stream(const fdgpu_ctx *ctx) { return (void *)ctx->stream; }
+extern "C" int fdh_ctx_fail(fdgpu_ctx *ctx, int cuda_error, const char *what)
+{
+    return cuda_fail(ctx, (cudaError_t)cuda_error, what);
+}
+
 extern "C" int fdgpu_velocity_to_slowness(fdgpu_ctx *ctx, const float *v, float *s, long long n, void *stream)
 {
     if (!ctx || (!v && n) || (!s && n) || n < 0) return FDGPU_EINVAL;

@@ -86,6 +86,31 @@ class ServeMetrics(C.Structure):
         return d
 
 
+class LocGrid(C.Structure):
+    """fdgpu_loc_grid: the grid and search parameters of sphfdloc's event location."""
+
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("x0", C.c_double), ("y0", C.c_double),
+                ("z0", C.c_double), ("h", C.c_double), ("dq", C.c_double), ("df", C.c_double),
+                ("xmax", C.c_float), ("ymax", C.c_float), ("zmax", C.c_float), ("z0r", C.c_double),
+                ("kmin", C.c_int), ("ndiv", C.c_int), ("ndiv2", C.c_int), ("ivs", C.c_int), ("vpvs", C.c_float),
+                ("nthres", C.c_int), ("resthres", C.c_float), ("resthrep", C.c_float), ("stdmax", C.c_float)]
+
+
+class LocObs(C.Structure):
+    """fdgpu_loc_obs: one phase of an event."""
+
+    _fields_ = [("field", C.c_int32), ("obstime", C.c_float), ("pwt", C.c_float), ("phase", C.c_char),
+                ("good", C.c_char), ("pad", C.c_char * 2)]
+
+
+class LocResult(C.Structure):
+    """fdgpu_loc_result."""
+
+    _fields_ = [("status", C.c_int32), ("ngood", C.c_int32), ("nxx", C.c_int32), ("nyy", C.c_int32),
+                ("nzz", C.c_int32), ("passes", C.c_int32), ("exm", C.c_double), ("eym", C.c_double),
+                ("ezm", C.c_double), ("stdmin", C.c_float), ("avrmin", C.c_float)]
+
+
 class FdgpuError(RuntimeError):
     pass
 
@@ -119,6 +144,12 @@ def load() -> C.CDLL:
         lib.fdgpu_velocity_to_slowness.argtypes = [P, C.c_void_p, C.c_void_p, C.c_longlong, C.c_void_p]
         lib.fdgpu_sphfd.argtypes = [C.c_int, C.POINTER(C.c_char_p), C.c_char_p]
         lib.fdgpu_sphfd_parlist.argtypes = [C.c_int, C.POINTER(C.c_char_p), C.c_char_p, C.POINTER(C.c_int)]
+        lib.fdgpu_loc_grid_from_spec.argtypes = [C.POINTER(LocGrid), C.c_int, C.c_int, C.c_int, C.c_double,
+                                                 C.c_double, C.c_double, C.c_double]
+        lib.fdgpu_loc_grid_from_spec.restype = None
+        lib.fdgpu_locate.argtypes = [P, C.POINTER(LocGrid), C.POINTER(C.c_void_p), C.c_int, C.c_int,
+                                     C.POINTER(C.c_int), C.POINTER(LocObs), C.POINTER(C.c_float),
+                                     C.POINTER(C.c_float), C.POINTER(LocResult), C.c_void_p]
         lib.fdgpu_serve_open.argtypes = [C.c_int, C.POINTER(ServeOpts), C.POINTER(P)]
         lib.fdgpu_serve_set_model.argtypes = [P, C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_int,
                                               C.POINTER(C.c_int)]
@@ -225,6 +256,42 @@ class Context:
     def velocity_to_slowness(self, vel_ptr: int, slow_ptr: int, n: int, stream_ptr: int = 0):
         _check(self.lib.fdgpu_velocity_to_slowness(self.ptr, C.c_void_p(vel_ptr), C.c_void_p(slow_ptr), n,
                                                    C.c_void_p(stream_ptr)), self.ptr)
+
+
+def loc_grid_from_spec(nx, ny, nz, x0_deg, y0_deg, z0_km, h_km) -> LocGrid:
+    """sphfdloc's grid from its spec values, with the reference's default search parameters."""
+    g = LocGrid()
+    load().fdgpu_loc_grid_from_spec(C.byref(g), nx, ny, nz, x0_deg, y0_deg, z0_km, h_km)
+    return g
+
+
+def locate(ctx: "Context", grid: LocGrid, field_ptrs, events, stream_ptr: int = 0):
+    """Locate events against device fields.  events: a list of phase lists, each phase
+    (field index, obstime, pwt, phase 'P'/'S', good).  Returns one dict per event with the result,
+    the final good flags, resmin and tps."""
+    lib = load()
+    offs = [0]
+    flat = []
+    for ev in events:
+        flat.extend(ev)
+        offs.append(len(flat))
+    n = len(flat)
+    obs = (LocObs * max(n, 1))(*[LocObs(f, t, w, ph.encode(), bytes([1 if g else 0])) for f, t, w, ph, g in flat])
+    off = (C.c_int * len(offs))(*offs)
+    fp = (C.c_void_p * max(len(field_ptrs), 1))(*field_ptrs)
+    resmin = (C.c_float * max(n, 1))()
+    tps = (C.c_float * max(n, 1))()
+    res = (LocResult * max(len(events), 1))()
+    _check(lib.fdgpu_locate(ctx.ptr, C.byref(grid), fp, len(field_ptrs), len(events), off, obs, resmin, tps, res,
+                            C.c_void_p(stream_ptr)), ctx.ptr)
+    out = []
+    for e in range(len(events)):
+        r = res[e]
+        a, b = offs[e], offs[e + 1]
+        out.append(dict(status=r.status, ngood=r.ngood, nxx=r.nxx, nyy=r.nyy, nzz=r.nzz, passes=r.passes,
+                        exm=r.exm, eym=r.eym, ezm=r.ezm, stdmin=r.stdmin, avrmin=r.avrmin,
+                        good=[obs[k].good[0] for k in range(a, b)], resmin=list(resmin[a:b]), tps=list(tps[a:b])))
+    return out
 
 
 def sphfd_parlist(entries, timedir: str):

@@ -14,6 +14,7 @@
  *      fdgpu_station_from_par, fdgpu_solve_host, fdgpu_solve_device, fdgpu_solve_noalloc.
  *   3. A serving session (fdgpu_serve_*): models resident on the device, requests admitted as
  *      they arrive and solved by a long-running grid, with latency statistics.
+ *   4. Consumers of the fields on the device: fdgpu_locate, sphfdloc's event location.
  *
  * Conventions: every function returns an FDGPU_* status (0 = success) and never aborts; the
  * caller owns host buffers and any device buffers it passes in; the library owns its scratch,
@@ -239,6 +240,62 @@ const char *fdgpu_serve_last_error(const fdgpu_server *sv);
 
 /* Complete every outstanding request, stop the grid and free the session. */
 int fdgpu_serve_close(fdgpu_server *sv);
+
+/* ---- Event location on device fields --------------------------------------------------------
+ *
+ * The grid search of FDtomoC's sphfdloc (src/sphfdloc.c) over travel-time fields that are already
+ * on the device (e.g. the fields a batch or a serving session just wrote): per event, a search over
+ * the grid nodes from depth index kmin (:729-794), two subgrid refinements with trilinear lookups
+ * (:840-1056, find_time :1305-1345), and the outlier / recovery passes that repeat the search
+ * (:1086-1128).  Results are bit-identical to the reference's; reading the event files and writing
+ * its report files stay with the caller. */
+typedef struct {
+    int nx, ny, nz;          /* the fields' grid */
+    double x0, y0, z0;       /* longitude of x = 0 (rad), geocentric colatitude of y = 0 (rad), depth of
+                                z = 0 (km) */
+    double h, dq, df;        /* depth step (km), colatitude and longitude steps (rad) */
+    float xmax, ymax, zmax;  /* far edges, as floats (src/sphfdloc.c:455-457) */
+    double z0r;              /* radius at z = 0 (km) */
+    int kmin;                /* first depth index of the node search (the spec's kmin - 1) */
+    int ndiv, ndiv2;         /* subdivisions of the two refinements */
+    int ivs;                 /* 0: an S time is the P field's time times vpvs */
+    float vpvs;
+    int nthres;              /* least number of accepted phases */
+    float resthres, resthrep, stdmax;
+} fdgpu_loc_grid;
+
+typedef struct {
+    int32_t field;           /* index of the phase's time field in d_fields */
+    float obstime;           /* arrival minus the event's catalogue origin time, s */
+    float pwt;               /* weight 1/(rwt*rwt) */
+    char phase;              /* 'P' or 'S' */
+    char good;               /* in: 0 for a phase marked '*'; out: the final flag */
+    char pad[2];
+} fdgpu_loc_obs;
+
+typedef struct {
+    int32_t status;          /* 0 accepted, 1 fewer than nthres phases left, 2 stdmin above stdmax */
+    int32_t ngood;           /* phases accepted */
+    int32_t nxx, nyy, nzz;   /* loop indices of the last improvement (0-based, as the reference's) */
+    int32_t passes;          /* searches run (1 + redos) */
+    double exm, eym, ezm;    /* hypocentre: longitude (rad), geocentric colatitude (rad), depth (km) */
+    float stdmin, avrmin;    /* deviation and mean residual there */
+} fdgpu_loc_result;
+
+/* The grid of a sphfdloc spec (src/sphfdloc.c:382-395): degrees and km in, and the reference's
+ * defaults for the search parameters (kmin 2, ndiv 20, ndiv2 20, ivs 1, vpvs 1.78, nthres 8,
+ * resthres 0.5, resthrep 5, stdmax 15). */
+void fdgpu_loc_grid_from_spec(fdgpu_loc_grid *g, int nx, int ny, int nz, double x0_deg, double y0_deg,
+                              double z0_km, double h_km);
+
+/* Locate nev events.  d_fields: device pointers to the time fields (nx*ny*nz floats each);
+ * obs_offset (nev + 1 entries, obs_offset[0] = 0): event e's phases are obs[obs_offset[e] ..
+ * obs_offset[e+1]), 1 to 800 of them; obs[].good is updated; resmin and tps (one per phase) receive
+ * the residuals and the computed times at the final point; results one per event.  Runs on `stream`
+ * (NULL: the context's) and returns when done. */
+int fdgpu_locate(fdgpu_ctx *ctx, const fdgpu_loc_grid *g, const float *const *d_fields, int nfields, int nev,
+                 const int *obs_offset, fdgpu_loc_obs *obs, float *resmin, float *tps, fdgpu_loc_result *results,
+                 void *stream);
 
 /* Drop-in sphfd(): ac/av as the reference's (av[1] = "par=<file>"), output_path = timedir.
  * Reads the velocity file, solves on the GPU, writes <output_path>/<timefile> byte-for-byte as

@@ -1,0 +1,112 @@
+"""Event location on device fields (fdgpu_locate) against the location oracle, and through it
+against the reference's own sphfdloc: the reference's output files of the golden cases are rebuilt
+byte for byte from the GPU's locations."""
+import numpy as np
+import pytest
+
+import loc_cases as LC
+from oracle_util import loc_grid, loc_helpers, oracle_locate
+
+KEYS = ("status", "ngood", "nxx", "nyy", "nzz", "passes", "exm", "eym", "ezm", "stdmin", "avrmin", "good",
+        "resmin", "tps")
+
+
+def gpu_grid(lib, p):
+    g = lib.loc_grid_from_spec(p["nx"], p["ny"], p["nz"], p["x0"], p["y0"], p["z0"], p["h"])
+    g.kmin, g.ndiv, g.ndiv2 = p["kmin"], p["ndiv"], p["ndiv2"]
+    g.nthres, g.resthres, g.resthrep, g.stdmax = p["nthres"], p["resthres"], p["resthrep"], p["stdmax"]
+    return g
+
+
+def same(a, b):
+    """bit equality of two result dicts (floats compared as their bits)"""
+    for k in KEYS:
+        x, y = a[k], b[k]
+        if isinstance(x, list):
+            if k in ("resmin", "tps"):
+                if not np.array_equal(np.asarray(x, np.float32).view(np.uint32), np.asarray(y, np.float32).view(np.uint32)):
+                    return k
+            elif list(x) != list(y):
+                return k
+        elif isinstance(x, float):
+            if np.float64(x).tobytes() != np.float64(y).tobytes():
+                return k
+        elif x != y:
+            return k
+    return None
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("seed", LC.SEEDS)
+def test_gpu_locations_equal_oracle_and_reference(gpu_lib, seed):
+    import torch
+    lib = gpu_lib
+    p, ref = LC.load_golden(seed)
+    grid_o = loc_grid(p)
+    ora = loc_helpers(grid_o)
+    fl = LC.fields(p)
+    keys = list(fl)
+    index = {k: i for i, k in enumerate(keys)}
+    dev = [torch.from_numpy(np.ascontiguousarray(fl[k])).cuda() for k in keys]
+    events = LC.parsed_events(p, ora["htoe"])
+    evobs = [[(index[(o["sta"], o["phase"])], o["obstime"], o["pwt"], o["phase"], 1) for o in ev["obs"]]
+             for ev in events]
+    with lib.Context(0) as ctx:
+        got = lib.locate(ctx, gpu_grid(lib, p), [t.data_ptr() for t in dev], evobs)
+    host = [np.ascontiguousarray(fl[k]) for k in keys]
+    want = [oracle_locate(grid_o, host, ob) for ob in evobs]
+    for e, (g_, w_) in enumerate(zip(got, want)):
+        assert same(g_, w_) is None, (e, same(g_, w_))
+    out = LC.format_outputs(p, events, got, ora)
+    for k in ("fhd", "sum", "dat", "out"):
+        assert out[k] == ref[k], k
+
+
+def random_case(seed, nx, ny, nz, ivs, nobs_max):
+    rng = np.random.default_rng(seed)
+    p = dict(seed=seed, nx=nx, ny=ny, nz=nz, h=1.0, x0=120.5, y0=24.0, z0=-2.0, kmin=int(rng.integers(0, 3)),
+             ndiv=int(rng.choice([5, 20])), ndiv2=int(rng.choice([5, 20])), nthres=int(rng.integers(5, 9)),
+             resthres=0.5, resthrep=5.0, stdmax=15.0, vp=6.0, vs=3.5)
+    p["stations"] = [dict(name=f"S{k:02d}", i=int(rng.integers(0, nx)), j=int(rng.integers(0, ny)), k=0)
+                     for k in range(int(rng.integers(6, 20)))]
+    fl = LC.fields(p)
+    keys = list(fl)
+    events = []
+    for _ in range(6):
+        hx, hy, hz = rng.uniform(0, nx - 1), rng.uniform(0, ny - 1), rng.uniform(0, nz - 1)
+        ob = []
+        for q, key in enumerate(keys):
+            if len(ob) >= nobs_max or rng.random() < 0.3:
+                continue
+            s = next(st for st in p["stations"] if st["name"] == key[0])
+            ph = key[1]
+            if ivs == 0 and ph == "S":
+                t = LC.travel_time(p, s, "P", hx, hy, hz) * 1.78
+            else:
+                t = LC.travel_time(p, s, ph, hx, hy, hz)
+            t += float(rng.normal(0, 0.03)) + (float(rng.choice([-2.0, 3.0])) if rng.random() < 0.1 else 0.0)
+            w = np.float32(rng.choice([0.05, 0.1, 0.3]))
+            fidx = keys.index((key[0], "P")) if (ivs == 0 and ph == "S") else q
+            ob.append((fidx, float(np.float32(t + 3.0)), float(np.float32(1.0) / (w * w)), ph,
+                       0 if rng.random() < 0.05 else 1))
+        events.append(ob)
+    return p, fl, keys, events
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("seed,shape,ivs", [(11, (31, 27, 19), 1), (12, (45, 38, 21), 0), (13, (61, 61, 31), 1)])
+def test_gpu_locations_random_cases(gpu_lib, seed, shape, ivs):
+    import torch
+    lib = gpu_lib
+    p, fl, keys, events = random_case(seed, *shape, ivs, 60)
+    grid_o = loc_grid(p)
+    grid_o.ivs = ivs
+    g = gpu_grid(lib, p)
+    g.ivs = ivs
+    dev = [torch.from_numpy(np.ascontiguousarray(fl[k])).cuda() for k in keys]
+    with lib.Context(0) as ctx:
+        got = lib.locate(ctx, g, [t.data_ptr() for t in dev], events)
+    host = [np.ascontiguousarray(fl[k]) for k in keys]
+    for e, ob in enumerate(events):
+        want = oracle_locate(grid_o, host, ob)
+        assert same(got[e], want) is None, (e, same(got[e], want))

@@ -40,3 +40,17 @@ def test_cases_exercise_the_outlier_passes():
         passes += sum(r["passes"] > 1 for r in results)
         rejected += sum(r["status"] != 0 for r in results)
     assert passes > 0 and rejected > 0
+
+
+def test_library_grid_setup_equals_oracle(gpu_lib):
+    """fdgpu_loc_grid_from_spec (host code, no GPU) and the oracle convert a spec identically."""
+    import ctypes as C
+    for seed in LC.SEEDS:
+        p, _ = LC.load_golden(seed)
+        a = loc_grid(p)
+        b = gpu_lib.loc_grid_from_spec(p["nx"], p["ny"], p["nz"], p["x0"], p["y0"], p["z0"], p["h"])
+        for name, _t in gpu_lib.LocGrid._fields_:
+            if name in ("kmin", "ndiv", "ndiv2", "nthres", "resthres", "resthrep", "stdmax"):
+                continue
+            x, y = getattr(a, name), getattr(b, name)
+            assert np.float64(x).tobytes() == np.float64(y).tobytes(), (seed, name, x, y)
