@@ -50,6 +50,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--serve-requests", type=int, default=300,
                     help="requests of the serving leg (0: skip it)")
+    ap.add_argument("--locate-events", type=int, default=256,
+                    help="events of the location leg (0: skip it)")
     args = ap.parse_args()
     if args.stations is None:
         args.stations = STATIONS_PER_GPU if args.config == 2 else 1
@@ -211,6 +213,89 @@ def serve_leg(args, lib, stations, v, batch_fields):
             "what": "all requests submitted at once; latency = submission to field ready on the device"}
 
 
+def locate_leg(args, lib, ctx, g, fields, stream):
+    """Event location (sphfdloc's grid search, fdgpu_locate) against the batch step's 64 P fields
+    still on the device: args.locate_events synthetic events, each with 24-40 picks taken from the
+    fields at a random grid node plus 20 ms noise and a few gross outliers.  Timed through the public
+    call (phases in from host memory, results out).  CPU baseline: the location oracle on the host
+    cores (one event per thread) for a sample of the events, whose results are also compared with the
+    GPU's bit for bit."""
+    import ctypes as C
+    from concurrent.futures import ThreadPoolExecutor
+    import numpy as np
+    import torch
+    E = args.locate_events
+    grid = lib.loc_grid_from_spec(g.nx, g.ny, g.nz, g.x0, g.y0, g.z0, g.h)
+    rng = np.random.default_rng(7)
+    ns = len(fields)
+    hyp = np.stack([rng.integers(0, g.nx, E), rng.integers(0, g.ny, E), rng.integers(grid.kmin, g.nz, E)], 1)
+    stack = torch.stack([f.reshape(-1) for f in fields])            # (ns, nxyz) on the device
+    node = torch.from_numpy((hyp[:, 2] * g.ny * g.nx + hyp[:, 1] * g.nx + hyp[:, 0]).astype(np.int64)).cuda()
+    tt = stack[:, node].T.cpu().numpy()                              # (E, ns) travel times
+    events = []
+    for e in range(E):
+        sel = rng.choice(ns, size=int(rng.integers(24, 41)), replace=False)
+        ob = []
+        for s_ in sel:
+            t = float(tt[e, s_]) + 5.0 + float(rng.normal(0, 0.02))
+            if rng.random() < 0.05:
+                t += float(rng.choice([-1.5, 2.5]))
+            w = np.float32(rng.choice([0.05, 0.1, 0.2]))
+            ob.append((int(s_), float(np.float32(t)), float(np.float32(1.0) / (w * w)), "P", 1))
+        events.append(ob)
+    ptrs = [f.data_ptr() for f in fields]
+    res = lib.locate(ctx, grid, ptrs, events[:8], stream.cuda_stream)   # warm-up
+    torch.cuda.synchronize()
+    t0 = time.time()
+    res = lib.locate(ctx, grid, ptrs, events, stream.cuda_stream)
+    gpu_s = time.time() - t0
+    nobs = sum(len(ob) for ob in events)
+
+    # CPU: the oracle, one event per host thread (ctypes releases the GIL during the call)
+    build_oracle()
+    olib = C.CDLL(os.path.join(ROOT, "oracle", "liboracle.so"))
+
+    class OObs(C.Structure):
+        _fields_ = [("field", C.c_int), ("obstime", C.c_float), ("pwt", C.c_float), ("phase", C.c_char),
+                    ("good", C.c_int)]
+    olib.fdo_locate.argtypes = [C.POINTER(lib.LocGrid), C.POINTER(C.POINTER(C.c_float)), C.c_int, C.POINTER(OObs),
+                                C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(lib.LocResult)]
+    host = [f.cpu().numpy().reshape(-1) for f in fields]
+    fp = (C.POINTER(C.c_float) * ns)(*[h.ctypes.data_as(C.POINTER(C.c_float)) for h in host])
+    cores = os.cpu_count() or 1
+    sample = list(range(min(E, cores)))
+
+    def one(e):
+        ob = events[e]
+        arr = (OObs * len(ob))(*[OObs(f, t, w, ph.encode(), gd) for f, t, w, ph, gd in ob])
+        rm = (C.c_float * len(ob))()
+        tp = (C.c_float * len(ob))()
+        r = lib.LocResult()
+        olib.fdo_locate(C.byref(grid), fp, len(ob), arr, rm, tp, C.byref(r))
+        return r, list(rm), [a.good for a in arr]
+
+    t0 = time.time()
+    with ThreadPoolExecutor(cores) as ex:
+        cpu = list(ex.map(one, sample))
+    cpu_s = time.time() - t0
+    mism = 0
+    for e, (r, rm, gd) in zip(sample, cpu):
+        a = res[e]
+        if (a["status"], a["nxx"], a["nyy"], a["nzz"], a["passes"], a["exm"], a["eym"], a["ezm"], a["stdmin"],
+                a["avrmin"]) != (r.status, r.nxx, r.nyy, r.nzz, r.passes, r.exm, r.eym, r.ezm, r.stdmin, r.avrmin) \
+                or np.asarray(a["resmin"], np.float32).tobytes() != np.asarray(rm, np.float32).tobytes() \
+                or list(a["good"]) != gd:
+            mism += 1
+    return {"events": E, "phases": nobs, "fields": ns, "grid": [g.nx, g.ny, g.nz],
+            "events_per_s": E / gpu_s, "wall_s": gpu_s,
+            "accepted": sum(1 for r in res if r["status"] == 0),
+            "passes_mean": sum(r["passes"] for r in res) / E,
+            "cpu_baseline": {"events_per_s": len(sample) / cpu_s, "cores": len(sample), "kind": "port",
+                             "sample": f"{len(sample)} of the {E} events, the location oracle, one event per host thread"},
+            "parity": {"events_checked": len(sample), "events_differing": mism, "bit_identical": mism == 0},
+            "what": "sphfdloc grid search (node search, two refinements, outlier passes) per event"}
+
+
 def run_gpu(args):
     rank, world, local = dist_env()
     n = args.stations
@@ -333,6 +418,7 @@ def run_gpu(args):
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         e2e["value"] = total_stations / float(t.item())
 
+    locating = locate_leg(args, lib, ctx, g, fields, stream) if args.locate_events > 0 else None
     serving = serve_leg(args, lib, stations, v, fields) if args.serve_requests > 0 else None
 
     # roofline of the solve kernel (one launch per step): algorithmic bytes 12 B per node update
@@ -379,6 +465,8 @@ def run_gpu(args):
         }
         if serving is not None:
             line["serving"] = serving
+        if locating is not None:
+            line["locate"] = locating
         if cpu is not None:
             line["cpu_baseline"] = cpu
         print(json.dumps(line), flush=True)

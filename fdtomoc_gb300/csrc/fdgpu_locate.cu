@@ -65,8 +65,17 @@ __device__ __forceinline__ unsigned long long trial_key(float std, unsigned idx)
     return ((unsigned long long)__float_as_uint(std) << 32) | idx;
 }
 
-/* trilinear time of the cell containing (x, yy, z), clamped to the grid (find_time, :1305-1345) */
-__device__ __forceinline__ double find_time(const fdgpu_loc_grid &g, const float *t, double x, double yy, double z)
+/* The cell containing (x, yy, z), clamped to the grid, and its eight trilinear weights, as find_time
+ * forms them (:1305-1345).  All fields share the grid, so a trial point computes these once for all
+ * its phases; each weight is the same product, in the same order, that the reference multiplies by
+ * the corner's time. */
+struct Cell {
+    long long a, b, a2, b2;
+    int i;
+    double w[8];
+};
+
+__device__ __forceinline__ void find_cell(const fdgpu_loc_grid &g, double x, double yy, double z, Cell &c)
 {
     int i = (int)((x - g.x0) / g.df);
     int j = (int)((yy - g.y0) / g.dq);
@@ -78,16 +87,34 @@ __device__ __forceinline__ double find_time(const fdgpu_loc_grid &g, const float
     j = j > g.ny - 2 ? g.ny - 2 : j;
     k = k > g.nz - 2 ? g.nz - 2 : k;
     const double xi = g.x0 + g.df * i, yj = g.y0 + g.dq * j, zk = g.z0 + g.h * k;
-    const int a = g.nx * g.ny * k, b = g.nx * j, a2 = g.nx * g.ny * (k + 1), b2 = g.nx * (j + 1);
+    c.a = (long long)g.nx * g.ny * k;
+    c.b = (long long)g.nx * j;
+    c.a2 = (long long)g.nx * g.ny * (k + 1);
+    c.b2 = (long long)g.nx * (j + 1);
+    c.i = i;
     const double fx = (x - xi) / g.df, fy = (yy - yj) / g.dq, fz = (z - zk) / g.h;
-    double tp = (1.0 - fx) * (1.0 - fy) * (1.0 - fz) * (double)t[a + b + i];
-    tp = tp + fx * (1.0 - fy) * (1.0 - fz) * (double)t[a + b + i + 1];
-    tp = tp + (1.0 - fx) * fy * (1.0 - fz) * (double)t[a + b2 + i];
-    tp = tp + (1.0 - fx) * (1.0 - fy) * fz * (double)t[a2 + b + i];
-    tp = tp + fx * fy * (1.0 - fz) * (double)t[a + b2 + i + 1];
-    tp = tp + fx * (1.0 - fy) * fz * (double)t[a2 + b + i + 1];
-    tp = tp + (1.0 - fx) * fy * fz * (double)t[a2 + b2 + i];
-    tp = tp + fx * fy * fz * (double)t[a2 + b2 + i + 1];
+    c.w[0] = (1.0 - fx) * (1.0 - fy) * (1.0 - fz);
+    c.w[1] = fx * (1.0 - fy) * (1.0 - fz);
+    c.w[2] = (1.0 - fx) * fy * (1.0 - fz);
+    c.w[3] = (1.0 - fx) * (1.0 - fy) * fz;
+    c.w[4] = fx * fy * (1.0 - fz);
+    c.w[5] = fx * (1.0 - fy) * fz;
+    c.w[6] = (1.0 - fx) * fy * fz;
+    c.w[7] = fx * fy * fz;
+}
+
+/* the trilinear time of one field in that cell: the reference's sum, term by term */
+__device__ __forceinline__ double cell_time(const Cell &c, const float *t)
+{
+    const int i = c.i;
+    double tp = c.w[0] * (double)t[c.a + c.b + i];
+    tp = tp + c.w[1] * (double)t[c.a + c.b + i + 1];
+    tp = tp + c.w[2] * (double)t[c.a + c.b2 + i];
+    tp = tp + c.w[3] * (double)t[c.a2 + c.b + i];
+    tp = tp + c.w[4] * (double)t[c.a + c.b2 + i + 1];
+    tp = tp + c.w[5] * (double)t[c.a2 + c.b + i + 1];
+    tp = tp + c.w[6] * (double)t[c.a2 + c.b2 + i];
+    tp = tp + c.w[7] * (double)t[c.a2 + c.b2 + i + 1];
     return tp;
 }
 
@@ -198,10 +225,12 @@ __global__ void __launch_bounds__(kLocBlock) loc_refine(fdgpu_loc_grid g, const 
     if (c < ncand) {
         const int i = (int)(c % ev.nsx), j = (int)((c / ev.nsx) % ev.nsy), k = (int)(c / ((long long)ev.nsx * ev.nsy));
         const double zp = ev.z0i + ev.sz * k, yp = ev.y0i + ev.sy * j, xp = ev.x0i + ev.sx * i;
+        Cell cell;
+        find_cell(g, xp, yp, zp, cell);
         float avres = 0.0f, rsq = 0.0f, facs = 0.0f;
         for (int q = 0; q < ev.nobs; q++) {
             const LocObsDev o{ot.field[q], ot.obstime[q], ot.pwt[q], ot.s_scaled[q]};
-            const float res = residual_d(o, find_time(g, o.field, xp, yp, zp), g.vpvs);
+            const float res = residual_d(o, cell_time(cell, o.field), g.vpvs);
             accumulate(res, ot.pwt[q], ot.good[q] != 0, avres, rsq, facs);
         }
         key = trial_key(deviation(avres, rsq, facs, ev.ngood), (unsigned)c);
@@ -305,6 +334,8 @@ __global__ void loc_finish(fdgpu_loc_grid g, const LocObsDev *obs, unsigned char
     float avres = 0.0f, rsq = 0.0f, facs = 0.0f;
     const bool found = ev.stdmin < INFINITY;
     const long long node = (long long)g.nx * g.ny * ev.nzz + (long long)g.nx * ev.nyy + ev.nxx;
+    Cell cell;
+    find_cell(g, ev.exm, ev.eym, ev.ezm, cell);
     for (int q = 0; q < ev.nobs; q++) {
         const int o = ev.obs0 + q;
         const LocObsDev d = obs[o];
@@ -312,7 +343,7 @@ __global__ void loc_finish(fdgpu_loc_grid g, const LocObsDev *obs, unsigned char
         if (ev.wstage == 0)
             res = d.s_scaled ? (float)((double)d.obstime - (double)d.field[node] * (double)g.vpvs) : d.obstime - d.field[node];
         else
-            res = residual_d(d, find_time(g, d.field, ev.exm, ev.eym, ev.ezm), g.vpvs);
+            res = residual_d(d, cell_time(cell, d.field), g.vpvs);
         accumulate(res, d.pwt, good[o] != 0, avres, rsq, facs);
         /* where no trial became the minimum in this pass the reference keeps the previous pass's
          * values (zero before the first) */
