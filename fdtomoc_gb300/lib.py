@@ -111,6 +111,14 @@ class LocResult(C.Structure):
                 ("ezm", C.c_double), ("stdmin", C.c_float), ("avrmin", C.c_float)]
 
 
+class C2fGrid(C.Structure):
+    """fdgpu_c2f_grid."""
+
+    _fields_ = [("nxc", C.c_int), ("nyc", C.c_int), ("nzc", C.c_int), ("igridx", C.POINTER(C.c_int)),
+                ("igridy", C.POINTER(C.c_int)), ("igridz", C.POINTER(C.c_int)), ("x0", C.c_double),
+                ("y0", C.c_double), ("z0", C.c_double), ("h", C.c_double)]
+
+
 class FdgpuError(RuntimeError):
     pass
 
@@ -150,6 +158,9 @@ def load() -> C.CDLL:
         lib.fdgpu_locate.argtypes = [P, C.POINTER(LocGrid), C.POINTER(C.c_void_p), C.c_int, C.c_int,
                                      C.POINTER(C.c_int), C.POINTER(LocObs), C.POINTER(C.c_float),
                                      C.POINTER(C.c_float), C.POINTER(LocResult), C.c_void_p]
+        lib.fdgpu_c2f_dims.argtypes = [C.POINTER(C2fGrid), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                       C.POINTER(C.c_int)]
+        lib.fdgpu_c2f.argtypes = [P, C.POINTER(C2fGrid), C.c_void_p, C.c_void_p, C.c_void_p]
         lib.fdgpu_serve_open.argtypes = [C.c_int, C.POINTER(ServeOpts), C.POINTER(P)]
         lib.fdgpu_serve_set_model.argtypes = [P, C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_int,
                                               C.POINTER(C.c_int)]
@@ -292,6 +303,27 @@ def locate(ctx: "Context", grid: LocGrid, field_ptrs, events, stream_ptr: int = 
                         exm=r.exm, eym=r.eym, ezm=r.ezm, stdmin=r.stdmin, avrmin=r.avrmin,
                         good=[obs[k].good[0] for k in range(a, b)], resmin=list(resmin[a:b]), tps=list(tps[a:b])))
     return out
+
+
+def c2f(ctx: "Context", nxc, nyc, nzc, igridx, igridy, igridz, x0, y0, z0, h, coarse, fine=None,
+        stream_ptr: int = 0):
+    """Coarse P/S velocities -> fine P/S velocities (c2f).  coarse: (2, nzc, nyc, nxc) float32 numpy
+    array or device tensor; fine: a (2, nz, ny, nx) buffer (numpy array or device tensor) or None for
+    a new numpy array.  Returns fine."""
+    import numpy as np
+    lib = load()
+    ix = (C.c_int * max(1, len(igridx)))(*igridx)
+    iy = (C.c_int * max(1, len(igridy)))(*igridy)
+    iz = (C.c_int * max(1, len(igridz)))(*igridz)
+    g = C2fGrid(nxc, nyc, nzc, ix, iy, iz, x0, y0, z0, h)
+    nx, ny, nz = C.c_int(), C.c_int(), C.c_int()
+    _check(lib.fdgpu_c2f_dims(C.byref(g), C.byref(nx), C.byref(ny), C.byref(nz)))
+    if fine is None:
+        fine = np.empty((2, nz.value, ny.value, nx.value), np.float32)
+    cp = coarse.ctypes.data if isinstance(coarse, np.ndarray) else coarse.data_ptr()
+    fp = fine.ctypes.data if isinstance(fine, np.ndarray) else fine.data_ptr()
+    _check(lib.fdgpu_c2f(ctx.ptr, C.byref(g), C.c_void_p(cp), C.c_void_p(fp), C.c_void_p(stream_ptr)), ctx.ptr)
+    return fine
 
 
 def sphfd_parlist(entries, timedir: str):

@@ -14,7 +14,8 @@
  *      fdgpu_station_from_par, fdgpu_solve_host, fdgpu_solve_device, fdgpu_solve_noalloc.
  *   3. A serving session (fdgpu_serve_*): models resident on the device, requests admitted as
  *      they arrive and solved by a long-running grid, with latency statistics.
- *   4. Consumers of the fields on the device: fdgpu_locate, sphfdloc's event location.
+ *   4. The path's neighbours on the device: fdgpu_c2f (c2f, the model's producer) and
+ *      fdgpu_locate (sphfdloc's event location, a consumer of the fields).
  *
  * Conventions: every function returns an FDGPU_* status (0 = success) and never aborts; the
  * caller owns host buffers and any device buffers it passes in; the library owns its scratch,
@@ -296,6 +297,25 @@ void fdgpu_loc_grid_from_spec(fdgpu_loc_grid *g, int nx, int ny, int nz, double 
 int fdgpu_locate(fdgpu_ctx *ctx, const fdgpu_loc_grid *g, const float *const *d_fields, int nfields, int nev,
                  const int *obs_offset, fdgpu_loc_obs *obs, float *resmin, float *tps, fdgpu_loc_result *results,
                  void *stream);
+
+/* ---- Coarse-to-fine model on the device ---------------------------------------------------------
+ *
+ * FDtomoC's c2f (src/c2f.c): the inversion's coarse P and S velocity nodes interpolated to the fine
+ * model sphfd reads, bit-identical to the reference's, so the model can go from the inversion to the
+ * solver without leaving the device. */
+typedef struct {
+    int nxc, nyc, nzc;                    /* coarse nodes per axis */
+    const int *igridx, *igridy, *igridz;  /* fine steps between neighbouring coarse nodes (nxc-1, ...) */
+    double x0, y0, z0, h;                 /* origin and fine spacing (the spec's x0, y0, z0, h) */
+} fdgpu_c2f_grid;
+
+/* fine dimensions: 1 + the sum of each axis's steps */
+int fdgpu_c2f_dims(const fdgpu_c2f_grid *g, int *nx, int *ny, int *nz);
+
+/* coarse velocities (P then S, nxc*nyc*nzc each, x fastest; host or device memory) to fine
+ * velocities (P then S, nx*ny*nz each; host or device memory), as c2f writes its .pvel and .svel
+ * files (src/c2f.c:541-572). */
+int fdgpu_c2f(fdgpu_ctx *ctx, const fdgpu_c2f_grid *g, const float *coarse, float *fine, void *stream);
 
 /* Drop-in sphfd(): ac/av as the reference's (av[1] = "par=<file>"), output_path = timedir.
  * Reads the velocity file, solves on the GPU, writes <output_path>/<timefile> byte-for-byte as

@@ -120,3 +120,28 @@ def oracle_locate(grid, field_list, obs):
     return dict(status=r.status, ngood=r.ngood, nxx=r.nxx, nyy=r.nyy, nzz=r.nzz, passes=r.passes, exm=r.exm,
                 eym=r.eym, ezm=r.ezm, stdmin=r.stdmin, avrmin=r.avrmin, good=[a.good for a in arr],
                 resmin=list(resmin), tps=list(tps))
+
+
+# ---- c2f oracle (oracle/fd_c2f.c) ------------------------------------------------------------
+
+class C2fGrid(C.Structure):
+    _fields_ = [("nxc", C.c_int), ("nyc", C.c_int), ("nzc", C.c_int), ("igridx", C.POINTER(C.c_int)),
+                ("igridy", C.POINTER(C.c_int)), ("igridz", C.POINTER(C.c_int)), ("x0", C.c_double),
+                ("y0", C.c_double), ("z0", C.c_double), ("h", C.c_double)]
+
+
+def oracle_c2f(p, coarse):
+    """coarse (2, nzc, nyc, nxc) float32 -> fine (2, nz, ny, nx) float32 by the oracle"""
+    import numpy as np
+    lib = load_oracle()
+    lib.fdo_c2f.argtypes = [C.POINTER(C2fGrid), C.POINTER(C.c_float), C.POINTER(C.c_float)]
+    ix = (C.c_int * len(p["igridx"]))(*p["igridx"])
+    iy = (C.c_int * len(p["igridy"]))(*p["igridy"])
+    iz = (C.c_int * len(p["igridz"]))(*p["igridz"])
+    g = C2fGrid(p["nxc"], p["nyc"], p["nzc"], ix, iy, iz, p["x0"], p["y0"], p["z0"], p["h"])
+    nx, ny, nz = 1 + sum(p["igridx"]), 1 + sum(p["igridy"]), 1 + sum(p["igridz"])
+    fine = np.empty((2, nz, ny, nx), np.float32)
+    src = np.ascontiguousarray(coarse, np.float32)
+    rc = lib.fdo_c2f(C.byref(g), src.ctypes.data_as(C.POINTER(C.c_float)), fine.ctypes.data_as(C.POINTER(C.c_float)))
+    assert rc == 0
+    return fine
