@@ -52,6 +52,7 @@ def parse():
                     help="requests of the serving leg (0: skip it)")
     ap.add_argument("--locate-events", type=int, default=256,
                     help="events of the location leg (0: skip it)")
+    ap.add_argument("--no-c2f", action="store_true", help="skip the c2f leg")
     args = ap.parse_args()
     if args.stations is None:
         args.stations = STATIONS_PER_GPU if args.config == 2 else 1
@@ -296,6 +297,73 @@ def locate_leg(args, lib, ctx, g, fields, stream):
             "what": "sphfdloc grid search (node search, two refinements, outlier passes) per event"}
 
 
+def c2f_leg(args, lib, ctx, stream):
+    """c2f (coarse-to-fine model) on the device: a 41x41x33 coarse P/S model onto the 401x401x161 fine
+    grid of the largest workload (25.9 M fine nodes per phase), through a plan (tables built once, as
+    an inversion loop reuses them), timed with CUDA events over repeated runs on its stream.  The
+    interpolation kernel writes 8 bytes per fine node (P and S) and reads a coarse model held in L2:
+    its roofline is HBM writes.  CPU baseline: the c2f oracle on one core (the reference's c2f is
+    single-threaded), and the GPU result's digest against the oracle's."""
+    import ctypes as C
+    import hashlib
+    import numpy as np
+    import torch
+    nxc, nyc, nzc = 41, 41, 33
+    ig = dict(igridx=[10] * (nxc - 1), igridy=[10] * (nyc - 1), igridz=[5] * (nzc - 1))
+    x0, y0, z0, h = -100.0, -100.0, -2.0, 0.5
+    rng = np.random.default_rng(5)
+    k, j, i = np.meshgrid(np.arange(nzc, dtype=np.float64), np.arange(nyc, dtype=np.float64),
+                          np.arange(nxc, dtype=np.float64), indexing="ij")
+    vp = 5.0 + 0.1 * k + 0.2 * rng.random((nzc, nyc, nxc))
+    coarse = np.stack([vp, vp / 1.73]).astype(np.float32)
+    plan = lib.C2fPlan(ctx, nxc, nyc, nzc, ig["igridx"], ig["igridy"], ig["igridz"], x0, y0, z0, h)
+    src = torch.from_numpy(coarse).cuda()
+    out = torch.empty(plan.shape, dtype=torch.float32, device="cuda")
+    nfine = out.numel() // 2
+    for _ in range(3):
+        plan.run(src.data_ptr(), out.data_ptr(), stream.cuda_stream)
+    reps = 20
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(reps):
+        plan.run(src.data_ptr(), out.data_ptr(), stream.cuda_stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    plan.close()
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    peak = peaks.get("hbm_gbs", 6800.0)
+    algo = 8.0 * nfine
+    gbs = algo / (ms * 1e-3) / 1e9
+    # CPU: the oracle on one core, and the digests
+    build_oracle()
+    olib = C.CDLL(os.path.join(ROOT, "oracle", "liboracle.so"))
+
+    class G(C.Structure):
+        _fields_ = lib.C2fGrid._fields_
+    olib.fdo_c2f.argtypes = [C.POINTER(G), C.POINTER(C.c_float), C.POINTER(C.c_float)]
+    arrs = [(C.c_int * len(ig[key]))(*ig[key]) for key in ("igridx", "igridy", "igridz")]
+    grid = G(nxc, nyc, nzc, *arrs, x0, y0, z0, h)
+    fine = np.empty(plan.shape, np.float32)
+    t0 = time.time()
+    olib.fdo_c2f(C.byref(grid), coarse.ctypes.data_as(C.POINTER(C.c_float)), fine.ctypes.data_as(C.POINTER(C.c_float)))
+    cpu_s = time.time() - t0
+    same = hashlib.sha256(out.cpu().numpy().tobytes()).hexdigest() == hashlib.sha256(fine.tobytes()).hexdigest()
+    return {"coarse": [nxc, nyc, nzc], "fine": list(plan.shape[:0:-1]), "ms_per_model": ms,
+            "fine_nodes_per_s": 2 * nfine / (ms * 1e-3),
+            "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+                         "algorithmic_bytes": algo, "note": "writes of the P and S fine models; the coarse model stays in L2"},
+            "cpu_baseline": {"ms_per_model": cpu_s * 1e3, "cores": 1, "kind": "port",
+                             "sample": "the whole model, the c2f oracle on one core"},
+            "parity": {"bit_identical": same},
+            "what": "c2f: coarse P/S velocities to the fine model sphfd reads, plan reused (fdgpu_c2f_run)"}
+
+
 def run_gpu(args):
     rank, world, local = dist_env()
     n = args.stations
@@ -419,6 +487,7 @@ def run_gpu(args):
         e2e["value"] = total_stations / float(t.item())
 
     locating = locate_leg(args, lib, ctx, g, fields, stream) if args.locate_events > 0 else None
+    modelling = c2f_leg(args, lib, ctx, stream) if not args.no_c2f else None
     serving = serve_leg(args, lib, stations, v, fields) if args.serve_requests > 0 else None
 
     # roofline of the solve kernel (one launch per step): algorithmic bytes 12 B per node update
@@ -467,6 +536,8 @@ def run_gpu(args):
             line["serving"] = serving
         if locating is not None:
             line["locate"] = locating
+        if modelling is not None:
+            line["c2f"] = modelling
         if cpu is not None:
             line["cpu_baseline"] = cpu
         print(json.dumps(line), flush=True)

@@ -38,29 +38,44 @@ __global__ void c2f_slowness(const float *v, float *s, int n)
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) s[i] = 1.f / v[i];
 }
 
-/* one thread per fine node and phase; blockIdx.y = phase */
-__global__ void __launch_bounds__(256) c2f_interp(const float *slow, const Axis *ax, const Axis *ay, const Axis *az,
-                                                  int nx, int ny, int nz, int nxc, int nyc, int nzc, float *out)
+/* Rows (phase, z, y) of the fine model go to warps, grid-stride; a warp's lanes take x = lane,
+ * lane + 32, ..., so each store instruction writes 128 contiguous bytes.  The grid is a few blocks
+ * per SM: the work is 2 nz ny rows of nx nodes, far too many short blocks otherwise. */
+constexpr int kC2fBlock = 256;
+
+__global__ void __launch_bounds__(kC2fBlock) c2f_interp(const float *__restrict__ slow, const Axis *__restrict__ ax,
+                                                        const Axis *__restrict__ ay, const Axis *__restrict__ az,
+                                                        int nx, int ny, int nz, int nxc, int nyc, int nzc,
+                                                        float *__restrict__ out)
 {
-    const long long nxyz = (long long)nx * ny * nz;
-    const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= nxyz) return;
-    const int ph = blockIdx.y;
-    const int i = (int)(n % nx), j = (int)((n / nx) % ny), k = (int)(n / ((long long)nx * ny));
-    const Axis X = ax[i], Y = ay[j], Z = az[k];
-    const float *sp = slow + (long long)ph * nxc * nyc * nzc;
-    const int a = nxc * nyc * Z.cell, b = nxc * Y.cell, a2 = nxc * nyc * (Z.cell + 1), b2 = nxc * (Y.cell + 1);
-    const int ci = X.cell;
-    const float fx = X.f, fy = Y.f, fz = Z.f, gx = X.omf, gy = Y.omf, gz = Z.omf;
-    float t = gx * gy * gz * sp[a + b + ci];
-    t = t + fx * gy * gz * sp[a + b + ci + 1];
-    t = t + gx * fy * gz * sp[a + b2 + ci];
-    t = t + gx * gy * fz * sp[a2 + b + ci];
-    t = t + fx * fy * gz * sp[a + b2 + ci + 1];
-    t = t + fx * gy * fz * sp[a2 + b + ci + 1];
-    t = t + gx * fy * fz * sp[a2 + b2 + ci];
-    t = t + fx * fy * fz * sp[a2 + b2 + ci + 1];
-    out[(long long)ph * nxyz + n] = 1.f / t;
+    const int lane = threadIdx.x & 31;
+    const long long rows = 2ll * nz * ny;
+    const long long nwarps = (long long)gridDim.x * (kC2fBlock / 32);
+    const long long ncoarse = (long long)nxc * nyc * nzc;
+    for (long long r = (long long)blockIdx.x * (kC2fBlock / 32) + (threadIdx.x >> 5); r < rows; r += nwarps) {
+        const int j = (int)(r % ny);
+        const int pk = (int)(r / ny);
+        const int ph = pk / nz, k = pk - ph * nz;
+        const Axis Y = ay[j], Z = az[k];
+        const float *sp = slow + ph * ncoarse;
+        const int a = nxc * nyc * Z.cell, b = nxc * Y.cell, a2 = nxc * nyc * (Z.cell + 1), b2 = nxc * (Y.cell + 1);
+        const float fy = Y.f, fz = Z.f, gy = Y.omf, gz = Z.omf;
+        float *row = out + r * nx;
+        for (int i = lane; i < nx; i += 32) {
+            const Axis X = ax[i];
+            const int ci = X.cell;
+            const float fx = X.f, gx = X.omf;
+            float t = gx * gy * gz * sp[a + b + ci];
+            t = t + fx * gy * gz * sp[a + b + ci + 1];
+            t = t + gx * fy * gz * sp[a + b2 + ci];
+            t = t + gx * gy * fz * sp[a2 + b + ci];
+            t = t + fx * fy * gz * sp[a + b2 + ci + 1];
+            t = t + fx * gy * fz * sp[a2 + b + ci + 1];
+            t = t + gx * fy * fz * sp[a2 + b2 + ci];
+            t = t + fx * fy * fz * sp[a2 + b2 + ci + 1];
+            row[i] = 1.f / t;
+        }
+    }
 }
 
 /* the per-axis entries: node coordinates accumulated as the reference does, fine positions rounded
@@ -123,61 +138,114 @@ extern "C" int fdgpu_c2f_dims(const fdgpu_c2f_grid *g, int *nx, int *ny, int *nz
     return FDGPU_OK;
 }
 
-#define C2F_CU(call)                                                        \
-    do {                                                                    \
-        const cudaError_t e_ = (call);                                      \
-        if (e_ != cudaSuccess) { rc = fdh_ctx_fail(ctx, (int)e_, #call); goto done; } \
-    } while (0)
+struct fdgpu_c2f_plan {
+    fdgpu_ctx *ctx = nullptr;
+    int device = 0;
+    int nx = 0, ny = 0, nz = 0, nxc = 0, nyc = 0, nzc = 0;
+    int sms = 0;
+    char *mem = nullptr;   /* slowness (2 x coarse), axis tables */
+    float *slow = nullptr;
+    Axis *ax = nullptr, *ay = nullptr, *az = nullptr;
+};
 
-extern "C" int fdgpu_c2f(fdgpu_ctx *ctx, const fdgpu_c2f_grid *g, const float *coarse, float *fine, void *stream)
+extern "C" int fdgpu_c2f_plan_create(fdgpu_ctx *ctx, const fdgpu_c2f_grid *g, fdgpu_c2f_plan **out)
 {
+    if (!ctx || !out) return FDGPU_EINVAL;
+    *out = nullptr;
     int nx, ny, nz;
-    if (!ctx || !coarse || !fine) return FDGPU_EINVAL;
     int rc = fdgpu_c2f_dims(g, &nx, &ny, &nz);
     if (rc) return rc;
     if (!(g->h > 0)) return FDGPU_EINVAL;
     const int dev = fdh_ctx_device(ctx);
     if (cudaSetDevice(dev) != cudaSuccess) return FDGPU_ENODEV;
-    cudaStream_t st = stream ? (cudaStream_t)stream : (cudaStream_t)fdh_ctx_stream(ctx);
-    bool cin = false, cout = false;
-    if (kind_of(coarse, dev, &cin) || kind_of(fine, dev, &cout)) return FDGPU_EINVAL;
-    const long long nxyz = (long long)nx * ny * nz;
-    const int nc2 = 2 * g->nxc * g->nyc * g->nzc;
     std::vector<Axis> ax, ay, az;
     axis_table(g->nxc, g->igridx, g->x0, g->h, nx, ax);
     axis_table(g->nyc, g->igridy, g->y0, g->h, ny, ay);
     axis_table(g->nzc, g->igridz, g->z0, g->h, nz, az);
-    /* one scratch allocation: coarse velocities (if on the host), slowness, axis tables, and the fine
-     * output (if on the host) */
-    const size_t off_v = 0, off_s = off_v + ((sizeof(float) * nc2 + 255) & ~(size_t)255);
-    const size_t off_x = off_s + ((sizeof(float) * nc2 + 255) & ~(size_t)255);
-    const size_t off_y = off_x + ((sizeof(Axis) * nx + 255) & ~(size_t)255);
-    const size_t off_z = off_y + ((sizeof(Axis) * ny + 255) & ~(size_t)255);
-    const size_t off_o = off_z + ((sizeof(Axis) * nz + 255) & ~(size_t)255);
-    const size_t total = off_o + (cout ? 0 : sizeof(float) * 2 * (size_t)nxyz);
-    char *mem = nullptr;
-    const float *vsrc;
-    float *dst;
-    C2F_CU(cudaMallocAsync((void **)&mem, total, st));
-    vsrc = cin ? coarse : reinterpret_cast<float *>(mem + off_v);
-    dst = cout ? fine : reinterpret_cast<float *>(mem + off_o);
-    if (!cin) C2F_CU(cudaMemcpyAsync(mem + off_v, coarse, sizeof(float) * nc2, cudaMemcpyHostToDevice, st));
-    C2F_CU(cudaMemcpyAsync(mem + off_x, ax.data(), sizeof(Axis) * nx, cudaMemcpyHostToDevice, st));
-    C2F_CU(cudaMemcpyAsync(mem + off_y, ay.data(), sizeof(Axis) * ny, cudaMemcpyHostToDevice, st));
-    C2F_CU(cudaMemcpyAsync(mem + off_z, az.data(), sizeof(Axis) * nz, cudaMemcpyHostToDevice, st));
-    c2f_slowness<<<(nc2 + 255) / 256 < 1024 ? (nc2 + 255) / 256 : 1024, 256, 0, st>>>(
-        vsrc, reinterpret_cast<float *>(mem + off_s), nc2);
-    c2f_interp<<<dim3((unsigned)((nxyz + 255) / 256), 2), 256, 0, st>>>(
-        reinterpret_cast<const float *>(mem + off_s), reinterpret_cast<const Axis *>(mem + off_x),
-        reinterpret_cast<const Axis *>(mem + off_y), reinterpret_cast<const Axis *>(mem + off_z), nx, ny, nz, g->nxc,
-        g->nyc, g->nzc, dst);
-    C2F_CU(cudaGetLastError());
-    if (!cout) C2F_CU(cudaMemcpyAsync(fine, dst, sizeof(float) * 2 * (size_t)nxyz, cudaMemcpyDeviceToHost, st));
-    C2F_CU(cudaStreamSynchronize(st));
-done:
-    if (mem) {
-        cudaFreeAsync(mem, st);
-        cudaStreamSynchronize(st);
+    auto *p = new (std::nothrow) fdgpu_c2f_plan;
+    if (!p) return FDGPU_ENOMEM;
+    p->ctx = ctx;
+    p->device = dev;
+    p->nx = nx; p->ny = ny; p->nz = nz;
+    p->nxc = g->nxc; p->nyc = g->nyc; p->nzc = g->nzc;
+    if (cudaDeviceGetAttribute(&p->sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || p->sms < 1) p->sms = 1;
+    const size_t nc2 = 2 * (size_t)g->nxc * g->nyc * g->nzc;
+    const size_t o_x = (sizeof(float) * nc2 + 255) & ~(size_t)255;
+    const size_t o_y = o_x + ((sizeof(Axis) * nx + 255) & ~(size_t)255);
+    const size_t o_z = o_y + ((sizeof(Axis) * ny + 255) & ~(size_t)255);
+    const size_t total = o_z + sizeof(Axis) * nz;
+    cudaError_t e = cudaMalloc((void **)&p->mem, total);
+    if (!e) e = cudaMemcpy(p->mem + o_x, ax.data(), sizeof(Axis) * nx, cudaMemcpyHostToDevice);
+    if (!e) e = cudaMemcpy(p->mem + o_y, ay.data(), sizeof(Axis) * ny, cudaMemcpyHostToDevice);
+    if (!e) e = cudaMemcpy(p->mem + o_z, az.data(), sizeof(Axis) * nz, cudaMemcpyHostToDevice);
+    if (e) {
+        rc = fdh_ctx_fail(ctx, (int)e, "c2f plan");
+        if (p->mem) cudaFree(p->mem);
+        delete p;
+        return rc;
     }
+    p->slow = reinterpret_cast<float *>(p->mem);
+    p->ax = reinterpret_cast<Axis *>(p->mem + o_x);
+    p->ay = reinterpret_cast<Axis *>(p->mem + o_y);
+    p->az = reinterpret_cast<Axis *>(p->mem + o_z);
+    *out = p;
+    return FDGPU_OK;
+}
+
+extern "C" int fdgpu_c2f_run(fdgpu_c2f_plan *p, const float *d_coarse, float *d_fine, void *stream)
+{
+    if (!p || !d_coarse || !d_fine) return FDGPU_EINVAL;
+    cudaStream_t st = stream ? (cudaStream_t)stream : (cudaStream_t)fdh_ctx_stream(p->ctx);
+    const int nc2 = 2 * p->nxc * p->nyc * p->nzc;
+    c2f_slowness<<<(nc2 + 255) / 256 < 1024 ? (nc2 + 255) / 256 : 1024, 256, 0, st>>>(d_coarse, p->slow, nc2);
+    const long long rows = 2ll * p->nz * p->ny;
+    const long long want = (rows + kC2fBlock / 32 - 1) / (kC2fBlock / 32);
+    const int blocks = (int)(want < (long long)p->sms * 8 ? want : (long long)p->sms * 8);
+    c2f_interp<<<blocks, kC2fBlock, 0, st>>>(p->slow, p->ax, p->ay, p->az, p->nx, p->ny, p->nz, p->nxc, p->nyc,
+                                              p->nzc, d_fine);
+    const cudaError_t e = cudaGetLastError();
+    return e ? fdh_ctx_fail(p->ctx, (int)e, "c2f launch") : FDGPU_OK;
+}
+
+extern "C" void fdgpu_c2f_plan_destroy(fdgpu_c2f_plan *p)
+{
+    if (!p) return;
+    cudaSetDevice(p->device);
+    if (p->mem) {
+        cudaDeviceSynchronize();
+        cudaFree(p->mem);
+    }
+    delete p;
+}
+
+extern "C" int fdgpu_c2f(fdgpu_ctx *ctx, const fdgpu_c2f_grid *g, const float *coarse, float *fine, void *stream)
+{
+    if (!ctx || !coarse || !fine) return FDGPU_EINVAL;
+    fdgpu_c2f_plan *p = nullptr;
+    int rc = fdgpu_c2f_plan_create(ctx, g, &p);
+    if (rc) return rc;
+    cudaStream_t st = stream ? (cudaStream_t)stream : (cudaStream_t)fdh_ctx_stream(ctx);
+    bool cin = false, cout = false;
+    const long long nxyz = (long long)p->nx * p->ny * p->nz;
+    const size_t nc2 = 2 * (size_t)p->nxc * p->nyc * p->nzc;
+    float *dc = nullptr, *df = nullptr;
+    cudaError_t e = cudaSuccess;
+    if (kind_of(coarse, p->device, &cin) || kind_of(fine, p->device, &cout)) {
+        fdgpu_c2f_plan_destroy(p);
+        return FDGPU_EINVAL;
+    }
+    if (!cin) {
+        e = cudaMallocAsync((void **)&dc, sizeof(float) * nc2, st);
+        if (!e) e = cudaMemcpyAsync(dc, coarse, sizeof(float) * nc2, cudaMemcpyHostToDevice, st);
+    }
+    if (!e && !cout) e = cudaMallocAsync((void **)&df, sizeof(float) * 2 * (size_t)nxyz, st);
+    if (!e) rc = fdgpu_c2f_run(p, cin ? coarse : dc, cout ? fine : df, st);
+    if (!e && !rc && !cout) e = cudaMemcpyAsync(fine, df, sizeof(float) * 2 * (size_t)nxyz, cudaMemcpyDeviceToHost, st);
+    if (dc) cudaFreeAsync(dc, st);
+    if (df) cudaFreeAsync(df, st);
+    const cudaError_t e2 = cudaStreamSynchronize(st);
+    if (!e) e = e2;
+    if (e && !rc) rc = fdh_ctx_fail(ctx, (int)e, "c2f");
+    fdgpu_c2f_plan_destroy(p);
     return rc;
 }

@@ -161,6 +161,10 @@ def load() -> C.CDLL:
         lib.fdgpu_c2f_dims.argtypes = [C.POINTER(C2fGrid), C.POINTER(C.c_int), C.POINTER(C.c_int),
                                        C.POINTER(C.c_int)]
         lib.fdgpu_c2f.argtypes = [P, C.POINTER(C2fGrid), C.c_void_p, C.c_void_p, C.c_void_p]
+        lib.fdgpu_c2f_plan_create.argtypes = [P, C.POINTER(C2fGrid), C.POINTER(P)]
+        lib.fdgpu_c2f_run.argtypes = [P, C.c_void_p, C.c_void_p, C.c_void_p]
+        lib.fdgpu_c2f_plan_destroy.argtypes = [P]
+        lib.fdgpu_c2f_plan_destroy.restype = None
         lib.fdgpu_serve_open.argtypes = [C.c_int, C.POINTER(ServeOpts), C.POINTER(P)]
         lib.fdgpu_serve_set_model.argtypes = [P, C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_int,
                                               C.POINTER(C.c_int)]
@@ -324,6 +328,36 @@ def c2f(ctx: "Context", nxc, nyc, nzc, igridx, igridy, igridz, x0, y0, z0, h, co
     fp = fine.ctypes.data if isinstance(fine, np.ndarray) else fine.data_ptr()
     _check(lib.fdgpu_c2f(ctx.ptr, C.byref(g), C.c_void_p(cp), C.c_void_p(fp), C.c_void_p(stream_ptr)), ctx.ptr)
     return fine
+
+
+class C2fPlan:
+    """fdgpu_c2f_plan: c2f onto one grid, repeatedly, with device buffers."""
+
+    def __init__(self, ctx: "Context", nxc, nyc, nzc, igridx, igridy, igridz, x0, y0, z0, h):
+        self.lib = load()
+        self.ctx = ctx
+        self._ig = [(C.c_int * max(1, len(a)))(*a) for a in (igridx, igridy, igridz)]
+        g = C2fGrid(nxc, nyc, nzc, *self._ig, x0, y0, z0, h)
+        nx, ny, nz = C.c_int(), C.c_int(), C.c_int()
+        _check(self.lib.fdgpu_c2f_dims(C.byref(g), C.byref(nx), C.byref(ny), C.byref(nz)))
+        self.shape = (2, nz.value, ny.value, nx.value)
+        self.ptr = C.c_void_p()
+        _check(self.lib.fdgpu_c2f_plan_create(ctx.ptr, C.byref(g), C.byref(self.ptr)), ctx.ptr)
+
+    def run(self, coarse_ptr: int, fine_ptr: int, stream_ptr: int = 0):
+        _check(self.lib.fdgpu_c2f_run(self.ptr, C.c_void_p(coarse_ptr), C.c_void_p(fine_ptr),
+                                      C.c_void_p(stream_ptr)), self.ctx.ptr)
+
+    def close(self):
+        if self.ptr:
+            self.lib.fdgpu_c2f_plan_destroy(self.ptr)
+            self.ptr = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def sphfd_parlist(entries, timedir: str):

@@ -317,6 +317,15 @@ int fdgpu_c2f_dims(const fdgpu_c2f_grid *g, int *nx, int *ny, int *nz);
  * files (src/c2f.c:541-572). */
 int fdgpu_c2f(fdgpu_ctx *ctx, const fdgpu_c2f_grid *g, const float *coarse, float *fine, void *stream);
 
+/* The same for a loop that interpolates a new coarse model onto one grid every iteration: the plan
+ * holds the grid's per-axis tables and the slowness scratch; fdgpu_c2f_run takes device buffers and
+ * only queues the two kernels on `stream` (NULL: the context's).  A plan is used by one stream at a
+ * time. */
+typedef struct fdgpu_c2f_plan fdgpu_c2f_plan;
+int fdgpu_c2f_plan_create(fdgpu_ctx *ctx, const fdgpu_c2f_grid *g, fdgpu_c2f_plan **out);
+int fdgpu_c2f_run(fdgpu_c2f_plan *plan, const float *d_coarse, float *d_fine, void *stream);
+void fdgpu_c2f_plan_destroy(fdgpu_c2f_plan *plan);
+
 /* Drop-in sphfd(): ac/av as the reference's (av[1] = "par=<file>"), output_path = timedir.
  * Reads the velocity file, solves on the GPU, writes <output_path>/<timefile> byte-for-byte as
  * the reference does.  Uses a per-thread default context on device 0. */

@@ -44,3 +44,21 @@ def test_gpu_c2f_equals_oracle_large(gpu_lib, seed):
         fine = run(gpu_lib, ctx, p, coarse, True)
     want = oracle_c2f(p, coarse)
     assert np.array_equal(fine.view(np.uint32), want.view(np.uint32))
+
+
+def test_gpu_c2f_plan_reused(gpu_lib):
+    """A plan interpolates successive coarse models (an inversion's iterations) like one-shot calls."""
+    import torch
+    g = GOLD["2"]
+    p = g["case"]
+    args = (p["nxc"], p["nyc"], p["nzc"], p["igridx"], p["igridy"], p["igridz"], p["x0"], p["y0"], p["z0"], p["h"])
+    with gpu_lib.Context(0) as ctx:
+        plan = gpu_lib.C2fPlan(ctx, *args)
+        out = torch.empty(plan.shape, dtype=torch.float32, device="cuda")
+        for it in range(3):
+            coarse = CC.coarse_model(p) * np.float32(1.0 + 0.01 * it)
+            src = torch.from_numpy(np.ascontiguousarray(coarse)).cuda()
+            plan.run(src.data_ptr(), out.data_ptr())
+            torch.cuda.synchronize()
+            assert np.array_equal(out.cpu().numpy().view(np.uint32), oracle_c2f(p, coarse).view(np.uint32))
+        plan.close()
