@@ -53,6 +53,8 @@ def parse():
     ap.add_argument("--locate-events", type=int, default=256,
                     help="events of the location leg (0: skip it)")
     ap.add_argument("--no-c2f", action="store_true", help="skip the c2f leg")
+    ap.add_argument("--profile-legs", action="store_true",
+                    help="only run a small fixed case of the c2f and location kernels (for ncu captures)")
     args = ap.parse_args()
     if args.stations is None:
         args.stations = STATIONS_PER_GPU if args.config == 2 else 1
@@ -364,6 +366,48 @@ def c2f_leg(args, lib, ctx, stream):
             "what": "c2f: coarse P/S velocities to the fine model sphfd reads, plan reused (fdgpu_c2f_run)"}
 
 
+def profile_legs(args):
+    """--profile-legs: a small fixed case of the c2f and location kernels for ncu captures (no timing,
+    no JSON line): c2f 41x41x33 -> 401x401x161 three times through a plan, then 32 events of 30 picks
+    located against 64 synthetic 201x201x81 fields (straight-ray times from surface stations)."""
+    import numpy as np
+    import torch
+    from fdtomoc_gb300 import build, lib as L
+    build.build()
+    ctx = L.Context(0)
+    nxc, nyc, nzc = 41, 41, 33
+    plan = L.C2fPlan(ctx, nxc, nyc, nzc, [10] * 40, [10] * 40, [5] * 32, -100.0, -100.0, -2.0, 0.5)
+    rng = np.random.default_rng(5)
+    vp = (5.0 + 0.2 * rng.random((nzc, nyc, nxc))).astype(np.float32)
+    src = torch.from_numpy(np.stack([vp, vp / 1.73]).astype(np.float32)).cuda()
+    out = torch.empty(plan.shape, dtype=torch.float32, device="cuda")
+    for _ in range(3):
+        plan.run(src.data_ptr(), out.data_ptr())
+    torch.cuda.synchronize()
+    plan.close()
+    del out
+    nx, ny, nz = 201, 201, 81
+    k, j, i = torch.meshgrid(torch.arange(nz, device="cuda", dtype=torch.float32),
+                             torch.arange(ny, device="cuda", dtype=torch.float32),
+                             torch.arange(nx, device="cuda", dtype=torch.float32), indexing="ij")
+    st = rng.integers(0, 201, (64, 2))
+    fields = [(torch.sqrt(((i - float(st[s_, 0])) * 0.5) ** 2 + ((j - float(st[s_, 1])) * 0.55) ** 2 + (k * 0.5) ** 2)
+               / 6.0).contiguous() for s_ in range(64)]
+    grid = L.loc_grid_from_spec(nx, ny, nz, 120.5, 23.5, -2.0, 0.5)
+    hyp = np.stack([rng.integers(0, nx, 32), rng.integers(0, ny, 32), rng.integers(2, nz, 32)], 1)
+    events = []
+    for e in range(32):
+        ob = []
+        for s_ in rng.choice(64, 30, replace=False):
+            t = float(fields[s_][hyp[e, 2], hyp[e, 1], hyp[e, 0]].item()) + 5.0 + float(rng.normal(0, 0.02))
+            ob.append((int(s_), float(np.float32(t)), 100.0, "P", 1))
+        events.append(ob)
+    res = L.locate(ctx, grid, [f.data_ptr() for f in fields], events)
+    torch.cuda.synchronize()
+    print("profile case done:", sum(r["status"] == 0 for r in res), "of", len(res), "events accepted")
+    ctx.close()
+
+
 def run_gpu(args):
     rank, world, local = dist_env()
     n = args.stations
@@ -589,7 +633,9 @@ def run_reference(args):
 
 def main():
     args = parse()
-    if args.impl == "reference":
+    if args.profile_legs:
+        profile_legs(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gpu(args)

@@ -199,11 +199,22 @@ __global__ void __launch_bounds__(kLocBlock) loc_coarse(fdgpu_loc_grid g, const 
     if (c < ncand) {
         const long long n = (long long)g.nx * g.ny * g.kmin + c;
         float avres = 0.0f, rsq = 0.0f, facs = 0.0f;
-        for (int q = 0; q < ev.nobs; q++) {
-            const float t = ot.field[q][n];
-            const float res = ot.s_scaled[q] ? (float)((double)ot.obstime[q] - (double)t * (double)g.vpvs)
-                                             : ot.obstime[q] - t;
-            accumulate(res, ot.pwt[q], ot.good[q] != 0, avres, rsq, facs);
+        /* the phases' times are loaded eight at a time, so that eight loads are in flight, and then
+         * accumulated in phase order */
+        constexpr int kBatch = 8;
+        for (int q0 = 0; q0 < ev.nobs; q0 += kBatch) {
+            float tv[kBatch];
+#pragma unroll
+            for (int u = 0; u < kBatch; u++) tv[u] = q0 + u < ev.nobs ? ot.field[q0 + u][n] : 0.0f;
+#pragma unroll
+            for (int u = 0; u < kBatch; u++) {
+                const int q = q0 + u;
+                if (q >= ev.nobs) break;
+                const float t = tv[u];
+                const float res = ot.s_scaled[q] ? (float)((double)ot.obstime[q] - (double)t * (double)g.vpvs)
+                                                 : ot.obstime[q] - t;
+                accumulate(res, ot.pwt[q], ot.good[q] != 0, avres, rsq, facs);
+            }
         }
         key = trial_key(deviation(avres, rsq, facs, ev.ngood), (unsigned)c);
     }
