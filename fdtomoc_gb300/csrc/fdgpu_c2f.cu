@@ -39,8 +39,8 @@ __global__ void c2f_slowness(const float *v, float *s, int n)
 }
 
 /* Rows (phase, z, y) of the fine model go to warps, grid-stride; a warp's lanes take x = lane,
- * lane + 32, ..., so each store instruction writes 128 contiguous bytes.  The grid is a few blocks
- * per SM: the work is 2 nz ny rows of nx nodes, far too many short blocks otherwise. */
+ * lane + 32, ..., so each store instruction writes 128 contiguous bytes.  The grid is one resident
+ * wave of blocks: the work is 2 nz ny rows of nx nodes, far too many short blocks otherwise. */
 constexpr int kC2fBlock = 256;
 
 __global__ void __launch_bounds__(kC2fBlock) c2f_interp(const float *__restrict__ slow, const Axis *__restrict__ ax,
@@ -142,7 +142,7 @@ struct fdgpu_c2f_plan {
     fdgpu_ctx *ctx = nullptr;
     int device = 0;
     int nx = 0, ny = 0, nz = 0, nxc = 0, nyc = 0, nzc = 0;
-    int sms = 0;
+    int sms = 0, per_sm = 1;   /* SMs, and interpolation blocks resident per SM */
     char *mem = nullptr;   /* slowness (2 x coarse), axis tables */
     float *slow = nullptr;
     Axis *ax = nullptr, *ay = nullptr, *az = nullptr;
@@ -169,6 +169,9 @@ extern "C" int fdgpu_c2f_plan_create(fdgpu_ctx *ctx, const fdgpu_c2f_grid *g, fd
     p->nx = nx; p->ny = ny; p->nz = nz;
     p->nxc = g->nxc; p->nyc = g->nyc; p->nzc = g->nzc;
     if (cudaDeviceGetAttribute(&p->sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || p->sms < 1) p->sms = 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p->per_sm, c2f_interp, kC2fBlock, 0) != cudaSuccess
+        || p->per_sm < 1)
+        p->per_sm = 1;
     const size_t nc2 = 2 * (size_t)g->nxc * g->nyc * g->nzc;
     const size_t o_x = (sizeof(float) * nc2 + 255) & ~(size_t)255;
     const size_t o_y = o_x + ((sizeof(Axis) * nx + 255) & ~(size_t)255);
@@ -200,7 +203,8 @@ extern "C" int fdgpu_c2f_run(fdgpu_c2f_plan *p, const float *d_coarse, float *d_
     c2f_slowness<<<(nc2 + 255) / 256 < 1024 ? (nc2 + 255) / 256 : 1024, 256, 0, st>>>(d_coarse, p->slow, nc2);
     const long long rows = 2ll * p->nz * p->ny;
     const long long want = (rows + kC2fBlock / 32 - 1) / (kC2fBlock / 32);
-    const int blocks = (int)(want < (long long)p->sms * 8 ? want : (long long)p->sms * 8);
+    const long long resident = (long long)p->sms * p->per_sm;   /* one wave: rows go to resident warps */
+    const int blocks = (int)(want < resident ? want : resident);
     c2f_interp<<<blocks, kC2fBlock, 0, st>>>(p->slow, p->ax, p->ay, p->az, p->nx, p->ny, p->nz, p->nxc, p->nyc,
                                               p->nzc, d_fine);
     const cudaError_t e = cudaGetLastError();
