@@ -45,8 +45,9 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--stations", type=int, default=None, help="stations per GPU (default 64; config 1: 1)")
-    ap.add_argument("--config", type=int, default=2, choices=[1, 2],
-                    help="2: the benchmark workload; 1: the one-station 61x61x31 case, for profiling")
+    ap.add_argument("--config", type=int, default=2, choices=[1, 2, 3],
+                    help="2: the benchmark workload; 1: the one-station 61x61x31 case, for profiling; "
+                         "3: the 500-window uneven batch (its own JSON line)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--serve-requests", type=int, default=300,
                     help="requests of the serving leg (0: skip it)")
@@ -408,6 +409,117 @@ def profile_legs(args):
     ctx.close()
 
 
+def run_config3(args):
+    """--config 3: the uneven-window batch.  500 station windows sized uniformly in 41..301 x 41..301 x
+    41..121 (seed 3) over the 401x401x161 model (seed 4), solved in one launch (largest windows
+    first), against the plain form (one window per launch, timed on a sample of windows).  Parity:
+    the sampled windows' batch fields equal their plain fields bit for bit, and the three smallest
+    windows equal the CPU oracle's fields.  Prints one JSON line."""
+    import numpy as np
+    import torch
+    from fdtomoc_gb300 import build, lib, workloads as W
+    from fdtomoc_gb300.formats import write_par
+    g, v, _ = W.config(3)
+    wins = W.config3_windows()
+    case_dir = tempfile.mkdtemp(prefix="fdbench_c3_")
+    W.write_case(case_dir, g, v, [])
+    velfile = os.path.join(case_dir, "vp.mod")
+    pars = []
+    for w in wins:
+        pf = os.path.join(case_dir, w["name"] + ".par")
+        write_par(pf, W.window_par(g, w, velfile, w["name"] + ".ptimes"))
+        pars.append(pf)
+    # CPU oracle on the three smallest windows, before any CUDA call in this process.  sphfd reads the
+    # first nx*ny*nz values of its velocity file, so each of these windows gets its own file, cut from
+    # the model where the GPU reads its window (ox, oy, 0)
+    from fdtomoc_gb300.formats import write_grid
+    sizes = [w["nx"] * w["ny"] * w["nz"] for w in wins]
+    small = sorted(range(len(wins)), key=lambda k: sizes[k])[:3]
+    for k in small:
+        w = wins[k]
+        wg = W.Grid(w["nx"], w["ny"], w["nz"], g.dlon, g.dlat, g.h, x0=g.x0 + w["ox"] * g.dlon,
+                    y0=g.y0 - w["oy"] * g.dlat, z0=g.z0)
+        wf = os.path.join(case_dir, w["name"] + ".mod")
+        write_grid(wf, W.head_for(wg), np.ascontiguousarray(v[:w["nz"], w["oy"]:w["oy"] + w["ny"], w["ox"]:w["ox"] + w["nx"]]))
+        write_par(pars[k], W.window_par(g, w, wf, w["name"] + ".ptimes"))
+    cpu_wall, cpu_nu, cpu_out = cpu_solve(case_dir, [wins[k]["name"] for k in small], 3)
+    build.build()
+    stations = []
+    for w, pf in zip(wins, pars):
+        st = lib.station_from_par("par=" + pf)[0]
+        st.ox, st.oy, st.oz = w["ox"], w["oy"], 0
+        stations.append(st)
+    ctx = lib.Context(0)
+    stream = torch.cuda.Stream()
+    vel_d = torch.from_numpy(v.reshape(-1)).cuda()
+    slow = torch.empty_like(vel_d)
+    ctx.velocity_to_slowness(vel_d.data_ptr(), slow.data_ptr(), v.size, stream.cuda_stream)
+    stream.synchronize()
+    del vel_d
+    fields = [torch.empty(st.shape, dtype=torch.float32, device="cuda") for st in stations]
+    ptrs = [f.data_ptr() for f in fields]
+
+    def batch():
+        return ctx.solve_device(stations, slow.data_ptr(), g.nx, g.nx * g.ny, ptrs, stream_ptr=stream.cuda_stream)
+
+    for _ in range(max(1, args.warmup)):
+        stats = batch()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    sampler = ClockSampler(0)
+    sampler.start()
+    e0.record(stream)
+    for _ in range(args.steps):
+        stats = batch()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    nu = sum(s_["node_updates"] for s_ in stats)
+    # plain: one window per launch, on a seeded sample
+    rng = np.random.default_rng(33)
+    sample = [int(k) for k in rng.choice(len(wins), 8, replace=False)]
+    plain_ms, same = [], 0
+    for k in sample:
+        out = torch.empty_like(fields[k])
+        e0.record(stream)
+        ctx.solve_device([stations[k]], slow.data_ptr(), g.nx, g.nx * g.ny, [out.data_ptr()],
+                         stream_ptr=stream.cuda_stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        plain_ms.append(e0.elapsed_time(e1))
+        same += int(torch.equal(out, fields[k]))
+    # the oracle's fields of the smallest windows
+    ora_same = 0
+    for k in small:
+        ref = np.fromfile(os.path.join(cpu_out, wins[k]["name"] + ".ptimes"), dtype="<f4", offset=232)
+        ora_same += int(np.array_equal(ref, fields[k].cpu().numpy().reshape(-1)))
+    plain_fps = 1e3 / (sum(plain_ms) / len(plain_ms))
+    line = {
+        "metric": "station fields/s (batched uneven windows, bit-identical to reference)", "value": len(wins) / (ms / 1e3),
+        "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": max(1, args.warmup), "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64 stencils / f32 fields",
+        "data": "synthetic (seeded, config 3 recipe)",
+        "config": {"workload": "500 windows 41..301 x 41..301 x 41..121 over a 401x401x161 model (config 3)",
+                   "windows": len(wins), "nodes": int(sum(sizes)), "launch_order": "largest windows first"},
+        "node_updates_per_s": nu / (ms / 1e3),
+        "latency_ms": {"p50": float(np.percentile([(s_["t_end_ns"] - min(x["t_start_ns"] for x in stats)) / 1e6 for s_ in stats], 50)),
+                       "p99": float(np.percentile([(s_["t_end_ns"] - min(x["t_start_ns"] for x in stats)) / 1e6 for s_ in stats], 99)),
+                       "what": "window completion time within the batch"},
+        "plain": {"sample_windows": len(sample), "ms_per_window_mean": sum(plain_ms) / len(plain_ms),
+                  "fields_per_s": plain_fps, "batched_over_plain": len(wins) / (ms / 1e3) / plain_fps},
+        "parity": {"sampled_windows_batch_equals_plain": f"{same}/{len(sample)}",
+                   "smallest_windows_equal_oracle": f"{ora_same}/{len(small)}"},
+        "cpu_baseline": {"value": len(small) / cpu_wall, "unit": UNIT, "cores": 3, "kind": "port",
+                         "sample": f"the {len(small)} smallest windows, one oracle process each (oracle FAST mode)"},
+        "clocks": clocks,
+        "gpu_launches": args.steps,
+    }
+    print(json.dumps(line), flush=True)
+    ctx.close()
+    shutil.rmtree(case_dir, ignore_errors=True)
+
+
 def run_gpu(args):
     rank, world, local = dist_env()
     n = args.stations
@@ -639,6 +751,8 @@ def main():
     args = parse()
     if args.profile_legs:
         profile_legs(args)
+    elif args.config == 3 and args.impl != "reference":
+        run_config3(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -279,6 +279,13 @@ extern "C" int fdgpu_solve_device(fdgpu_ctx *ctx, int n, const fdgpu_station *st
                           ctx->trig.as<double>() + (size_t)maxt * k, ctx->stats.as<fd_station_stats>() + k);
         max_pad = std::max(max_pad, hs[k].max_face_pad);
     }
+    /* Launch order: largest grids first.  CTA i solves record i, and CTAs beyond the resident ones
+     * start as earlier ones finish, so a batch of uneven windows ends sooner when the long solves
+     * start first (longest-processing-time order).  Each record keeps its own statistics slot, so
+     * the caller's order is unaffected. */
+    std::stable_sort(hs.begin(), hs.end(), [](const fd_station_dev &a, const fd_station_dev &b) {
+        return (long long)a.g.nx * a.g.ny * a.g.nz > (long long)b.g.nx * b.g.ny * b.g.nz;
+    });
     FD_CU(ctx, cudaMemcpyAsync(ctx->trig.p, trig.data(), sizeof(double) * trig.size(), cudaMemcpyHostToDevice, cs));
     FD_CU(ctx, cudaMemcpyAsync(ctx->stations.p, hs.data(), sizeof(fd_station_dev) * n, cudaMemcpyHostToDevice, cs));
     FD_CU(ctx, fdk_launch_solve(ctx->stations.as<fd_station_dev>(), n, max_pad, ctx->cluster, cs));

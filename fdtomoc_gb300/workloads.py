@@ -115,10 +115,23 @@ def config(n: int):
     if n == 2:
         g = Grid(201, 201, 81, 0.005, 0.005, 0.5)
         return g, layered_model(g, 0.05, 10.0, 2), stations(g, 64, 2)
+    if n == 3:
+        g = Grid(401, 401, 161, 0.005, 0.005, 0.5)
+        return g, layered_model(g, 0.05, 10.0, 4), []
     if n == 5:
         g = Grid(401, 401, 161, 0.005, 0.005, 0.5)
         return g, add_slab(g, layered_model(g, 0.05, 10.0, 5)), stations(g, 1200, 5)
     raise ValueError(n)
+
+
+def window_par(grid: Grid, w: dict, velfile: str, timefile: str) -> dict:
+    """Par values of a config-3 window: its own grid, its north-west corner at (ox, oy) of the model,
+    z from the model's top, and a surface station at (fx, fy) of the window."""
+    x0 = grid.x0 + w["ox"] * grid.dlon
+    y0 = grid.y0 - w["oy"] * grid.dlat
+    st = dict(lon=x0 + w["fx"] * grid.dlon, lat=y0 - w["fy"] * grid.dlat, elev=w["elev"])
+    g = Grid(w["nx"], w["ny"], w["nz"], grid.dlon, grid.dlat, grid.h, x0=x0, y0=y0, z0=grid.z0)
+    return par_for(g, st, velfile, timefile)
 
 
 def config3_windows(n_windows: int = 500, seed: int = 3):
