@@ -45,9 +45,10 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--stations", type=int, default=None, help="stations per GPU (default 64; config 1: 1)")
-    ap.add_argument("--config", type=int, default=2, choices=[1, 2, 3],
+    ap.add_argument("--rate", type=float, default=12.0, help="--config 4: request arrivals per second")
+    ap.add_argument("--config", type=int, default=2, choices=[1, 2, 3, 4],
                     help="2: the benchmark workload; 1: the one-station 61x61x31 case, for profiling; "
-                         "3: the 500-window uneven batch (its own JSON line)")
+                         "3: the 500-window uneven batch; 4: served P/S requests (each its own JSON line)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--serve-requests", type=int, default=300,
                     help="requests of the serving leg (0: skip it)")
@@ -520,6 +521,95 @@ def run_config3(args):
     shutil.rmtree(case_dir, ignore_errors=True)
 
 
+def run_config4(args):
+    """--config 4: served P and S solves.  Requests (station window, phase) drawn from 800 windows
+    (61..301 x 61..301 x 61..121 over the 401x401x161 model, seed 4) arrive as a seeded Poisson stream
+    (args.rate per second); S = P/1.73 with an independent 2 % perturbation; every 100 requests both
+    models are replaced by a 1 % smooth perturbation of themselves, as an inversion iteration would.
+    Reports throughput, latency percentiles and, for a sample of requests, bit equality with the same
+    station solved alone against the model version it was served with.  Prints one JSON line."""
+    import numpy as np
+    import torch
+    from fdtomoc_gb300 import build, lib, workloads as W
+    from fdtomoc_gb300.formats import write_par
+    g, vp, _ = W.config(3)
+    vs = (vp / 1.73 * (1.0 + 0.02 * W.smooth_noise(vp.shape, (g.h, 0.556, 0.509), 10.0, 41))).astype(np.float32)
+    rng = np.random.default_rng(4)
+    wins = []
+    for i in range(800):
+        wx, wy, wz = int(rng.integers(61, 302)), int(rng.integers(61, 302)), int(rng.integers(61, 122))
+        ox, oy = int(rng.integers(0, 401 - wx + 1)), int(rng.integers(0, 401 - wy + 1))
+        wins.append(dict(name=f"R{i:04d}", nx=wx, ny=wy, nz=wz, ox=ox, oy=oy, fx=float(rng.uniform(2, wx - 3)),
+                         fy=float(rng.uniform(2, wy - 3)), elev=float(rng.uniform(0, 2))))
+    case_dir = tempfile.mkdtemp(prefix="fdbench_c4_")
+    build.build()
+    stations = []
+    for w in wins:
+        pf = os.path.join(case_dir, w["name"] + ".par")
+        write_par(pf, W.window_par(g, w, os.path.join(case_dir, "vp.mod"), w["name"] + ".ptimes"))
+        st = lib.station_from_par("par=" + pf)[0]
+        st.ox, st.oy, st.oz = w["ox"], w["oy"], 0
+        stations.append(st)
+    n = args.serve_requests
+    picks = [(int(rng.integers(0, 800)), int(rng.integers(0, 2))) for _ in range(n)]
+    gaps = rng.exponential(1.0 / args.rate, n)
+    # the model versions, made before the clock starts
+    versions = {0: [vp], 1: [vs]}
+    for q in range(100, n, 100):
+        for m_ in (0, 1):
+            pert = W.smooth_noise(vp.shape, (g.h, 0.556, 0.509), 10.0, 1000 + q + m_)
+            versions[m_].append((versions[m_][-1] * (1.0 + 0.01 * pert)).astype(np.float32))
+    outs = [torch.empty(stations[k].shape, dtype=torch.float32, device="cuda") for k, _ in picks]
+    meta = []
+    with lib.Server(0, hbm_bytes=120 << 30) as sv:
+        sv.set_model(0, vp)
+        sv.set_model(1, vs)
+        cur = {0: 1, 1: 1}
+        t0 = time.time()
+        due = t0
+        for q, (k, ph) in enumerate(picks):
+            if q > 0 and q % 100 == 0:
+                for m_ in (0, 1):
+                    sv.set_model(m_, versions[m_][cur[m_]])
+                    cur[m_] += 1
+            due += gaps[q]
+            d = due - time.time()
+            if d > 0:
+                time.sleep(d)
+            sv.submit(stations[k], ph, outs[q], tag=q)
+            meta.append((k, ph, cur[ph]))
+        sv.drain(3600000)
+        wall = time.time() - t0
+        res = sv.poll(n + 8)
+        m = sv.metrics()
+    bad = sum(1 for r in res if r["status"] != 0)
+    # a sample re-solved alone against the model version each was served with
+    sample = [int(q) for q in np.random.default_rng(44).choice(n, 6, replace=False)]
+    same = 0
+    with lib.Context(0) as ctx:
+        for q in sample:
+            k, ph, ver = meta[q]
+            v = versions[ph][ver - 1]
+            (t,), _ = ctx.solve_host([stations[k]], v)
+            same += int(np.array_equal(t.view(np.uint32), outs[q].cpu().numpy().view(np.uint32)))
+    line = {
+        "metric": "station fields/s served (P and S, Poisson arrivals), bit-identical to reference",
+        "value": n / wall, "unit": UNIT, "n_gpus": 1, "steps": 1, "warmup": 0, "ms_per_step": wall * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64 stencils / f32 fields",
+        "data": "synthetic (seeded, config 4 recipe, scaled rate)",
+        "config": {"workload": f"{n} requests over 800 windows 61..301 x 61..301 x 61..121 (401x401x161 model), "
+                               f"P and S, Poisson {args.rate}/s, models replaced every 100 requests (config 4)",
+                   "rate_per_s": args.rate, "model_updates": cur[0] - 1},
+        "latency_ms": {"p50": m["p50_ms"], "p90": m["p90_ms"], "p99": m["p99_ms"], "max": m["max_ms"]},
+        "solve_ms": {"p50": m["solve_p50_ms"], "p99": m["solve_p99_ms"]},
+        "node_updates_per_s": m["node_updates"] / wall, "failed": bad, "hbm_peak_bytes": m["hbm_peak"],
+        "parity": {"sampled_requests_equal_alone": f"{same}/{len(sample)}"},
+        "gpu_launches": m["grid_launches"],
+    }
+    print(json.dumps(line), flush=True)
+    shutil.rmtree(case_dir, ignore_errors=True)
+
+
 def run_gpu(args):
     rank, world, local = dist_env()
     n = args.stations
@@ -753,6 +843,8 @@ def main():
         profile_legs(args)
     elif args.config == 3 and args.impl != "reference":
         run_config3(args)
+    elif args.config == 4 and args.impl != "reference":
+        run_config4(args)
     elif args.impl == "reference":
         run_reference(args)
     else:
