@@ -72,3 +72,80 @@ def write_random_case(case: dict, dirname: str) -> str:
     pf = os.path.join(dirname, "case.par")
     write_par(pf, par)
     return pf
+
+
+START_KINDS = ("oldt", "walls", "box")
+
+
+def start_case(seed: int, kind: str) -> dict:
+    """A random case turned into a solve from a supplied start: "oldt" (srctype 3: a whole starting
+    field, times on the source wall's layer and 1e10 elsewhere), "walls" (srctype 2: a wall file of six
+    records, the valid ones starting above -1e-20) or "box" (srctype 1 with fill=1: the source box's
+    times from a box file).  The supplied times are straight-line times from a seeded node, made with
+    +, *, / and sqrt only, so they are the same on every machine.  Returns the case with its extra
+    files under "files" (name -> bytes)."""
+    c = random_case(seed)
+    p = dict(c["par"])
+    nx, ny, nz = p["nx"], p["ny"], p["nz"]
+    rng = np.random.default_rng(seed + 7000)
+    i0, j0, k0 = (int(rng.integers(0, n)) for n in (nx, ny, nz))
+    kk, jj, ii = np.meshgrid(np.arange(nz, dtype=np.float64), np.arange(ny, dtype=np.float64),
+                             np.arange(nx, dtype=np.float64), indexing="ij")
+    base = (np.sqrt(((ii - i0) * 1.1) ** 2 + ((jj - j0) * 1.05) ** 2 + ((kk - k0) * p["h"]) ** 2) / 6.0 + 0.25
+            ).astype(np.float32)
+    files = {}
+    if kind in ("oldt", "walls"):
+        for key in ("fxs", "fys", "fzs", "xs", "ys", "zs", "floatsrc", "NCUBE"):
+            p.pop(key, None)
+        srcwall = int(rng.integers(1, 7))
+        p["srctype"] = 3 if kind == "oldt" else 2
+        p["srcwall"] = srcwall
+        # the layer of srcwall (src/sphfd.c:877-926): 1 x=0, 2 x=nx-1, 3 y=0, 4 y=ny-1, 5 z=0, 6 z=nz-1
+        sel = [np.s_[:, :, 0], np.s_[:, :, nx - 1], np.s_[:, 0, :], np.s_[:, ny - 1, :], np.s_[0, :, :],
+               np.s_[nz - 1, :, :]]
+        if kind == "oldt":
+            t = np.full((nz, ny, nx), 1.0e10, np.float32)
+            t[sel[srcwall - 1]] = base[sel[srcwall - 1]]
+            files["oldt.bin"] = t.tobytes()
+            p["oldtfile"] = "@oldt.bin"
+        else:
+            nwall = ny * nz if (nx <= ny and nx <= nz) else (nx * nz if (ny <= nx and ny <= nz) else nx * ny)
+            recs = []
+            extra = int(rng.integers(0, 6))
+            for w in range(6):
+                rec = np.full(nwall, -1.0, np.float32)
+                if w == srcwall - 1 or w == extra:
+                    vals = base[sel[w]].reshape(-1)   # wall order: (k, j) for x walls, (k, i) for y, (j, i) for z
+                    rec[:vals.size] = vals
+                recs.append(rec)
+            files["walls.bin"] = np.concatenate(recs).tobytes()
+            p["wallfile"] = "@walls.bin"
+    elif kind == "box":
+        nc = int(p.get("NCUBE", 2))
+        w = 2 * nc + 1
+        box = (0.05 + 0.01 * np.arange(w ** 3, dtype=np.float64) % 0.7).astype(np.float32)
+        head = VHead(header=b"HEADFINESPHRPTIMbox", nx=w, ny=w, nz=w, dz=p["h"])
+        files["box.bin"] = head.pack() + box.tobytes()
+        p["fill"] = 1
+        p["boxfile"] = "@box.bin"
+    else:
+        raise ValueError(kind)
+    c = dict(c, par=p, files=files, kind=kind)
+    return c
+
+
+def write_start_case(case: dict, dirname: str) -> str:
+    """Write a start_case: its files, then model and par file with '@name' values pointing at them."""
+    os.makedirs(dirname, exist_ok=True)
+    par = dict(case["par"])
+    for name, data in case["files"].items():
+        path = os.path.join(dirname, name)
+        with open(path, "wb") as f:
+            f.write(data)
+        for k, v in list(par.items()):
+            if v == "@" + name:
+                par[k] = path
+    return write_random_case(dict(case, par=par), dirname)
+
+
+START_SEEDS = (3, 8, 14, 27, 40, 61)

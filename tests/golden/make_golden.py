@@ -12,7 +12,8 @@ Writes:
                     restored at data offsets 103421, 131353, 181824; checked against a fresh run of the
                     reference binary.
   reference_outputs.json
-                    SHA-256 of the reference binary's time file for seeded cases (cases.py) and for
+                    SHA-256 of the reference binary's time file for seeded cases (cases.py), for
+                    solves from a supplied start (srctype 2 and 3, fill=1; cases.start_case) and for
                     config 1 (fdtomoc_gb300.workloads), with their sweep counts.
 """
 import hashlib
@@ -87,6 +88,22 @@ def main():
         b = open(os.path.join(d, "out", "case.ptimes"), "rb").read()
         cases[str(s)] = {"sha256": hashlib.sha256(b).hexdigest(), "sweeps": sweeps_of(log), "bytes": len(b)}
     out["cases"] = cases
+    # solves from a supplied start (srctype 2, srctype 3, fill=1)
+    from cases import START_KINDS, START_SEEDS, start_case, write_start_case
+    starts = {}
+    for s in START_SEEDS:
+        for kind in START_KINDS:
+            d = os.path.join(tmp, f"s{s}_{kind}")
+            pf = write_start_case(start_case(s, kind), d)
+            log = run_reference(pf, os.path.join(d, "out"))
+            b = open(os.path.join(d, "out", "case.ptimes"), "rb").read()
+            # srctype 2/3: the reference writes its uninitialised source point into the header's
+            # fxs/fys/fzs (bytes 120-143), so those cases are compared with the three doubles zeroed
+            masked = b[:120] + bytes(24) + b[144:]
+            starts[f"{s}_{kind}"] = {"sha256": hashlib.sha256(b).hexdigest(),
+                                     "sha256_source_zeroed": hashlib.sha256(masked).hexdigest(),
+                                     "sweeps": sweeps_of(log), "bytes": len(b)}
+    out["start_cases"] = starts
     # config 1
     from fdtomoc_gb300 import workloads as W
     g, v, sts = W.config(1)

@@ -33,3 +33,17 @@ def test_seeded_cases_reference_hash(gpu_lib, tmp_path, seed):
     assert gpu_lib.sphfd_parlist([f"par={pf}"], str(tmp_path / "out")) == [0]
     got = hashlib.sha256((tmp_path / "out" / "case.ptimes").read_bytes()).hexdigest()
     assert got == REF["cases"][str(seed)]["sha256"]
+
+
+@pytest.mark.parametrize("key", sorted(REF["start_cases"]))
+def test_start_cases_reference_hash(gpu_lib, tmp_path, key):
+    """srctype 3 (starting field), srctype 2 (wall file) and fill=1 (box file) through the drop-in,
+    against the reference binary's time files."""
+    from cases import start_case, write_start_case
+    seed, kind = key.split("_")
+    pf = write_start_case(start_case(int(seed), kind), str(tmp_path))
+    os.makedirs(tmp_path / "out")
+    assert gpu_lib.sphfd_parlist([f"par={pf}"], str(tmp_path / "out")) == [0]
+    b = (tmp_path / "out" / "case.ptimes").read_bytes()
+    want = REF["start_cases"][key]["sha256" if kind == "box" else "sha256_source_zeroed"]
+    assert hashlib.sha256(b).hexdigest() == want   # srctype 2/3: header source point written as zeros
