@@ -34,6 +34,8 @@ def make_case(seed: int) -> dict:
              igridz=[gz] * (nzc - 1), nx=nx, ny=ny, nz=nz, h=h, x0=120.5, y0=24.0, z0=-2.0,
              kmin=2, ndiv=int(rng.choice([4, 10, 20])), ndiv2=int(rng.choice([4, 10, 20])), nthres=6,
              resthres=0.5, resthrep=5.0, stdmax=15.0, vp=6.0, vs=3.5)
+    if seed >= 5:
+        p["ivs"], p["vpvs"] = 0, 1.75   # S times taken as the S field's times x vpvs (:745-747)
     nst = int(rng.integers(8, 14))
     p["stations"] = [dict(name=f"S{k:02d}", i=int(rng.integers(0, nx)), j=int(rng.integers(0, ny)), k=0)
                      for k in range(nst)]
@@ -46,6 +48,8 @@ def make_case(seed: int) -> dict:
                 if rng.random() < 0.2:
                     continue
                 tt = travel_time(p, s, ph, hx, hy, hz)
+                if ph == "S" and p.get("ivs") == 0:
+                    tt *= p["vpvs"]   # consistent with how ivs 0 reads an S time
                 noise = float(rng.normal(0, 0.02))
                 if rng.random() < 0.08:
                     noise += float(rng.choice([-1.5, 2.5]))   # a gross outlier
@@ -83,11 +87,6 @@ def fields(p):
     return {(s["name"], ph): field(p, s, ph) for s in p["stations"] for ph in ("P", "S")}
 
 
-def _epoch_parts(t):
-    """(year, jday, hour, minute, sec) of an absolute time in days of 2020 + seconds."""
-    return t
-
-
 def event_text(p) -> str:
     """The event list the reference reads (leqsfil): a header line per event, one line per pick
     with its absolute arrival time, a blank line after each event."""
@@ -111,6 +110,8 @@ def spec_text(p, d) -> str:
              f"resthres {p['resthres']}", f"resthrep {p['resthrep']}", f"stdmax {p['stdmax']}",
              "igridx " + " ".join(map(str, p["igridx"])), "igridy " + " ".join(map(str, p["igridy"])),
              "igridz " + " ".join(map(str, p["igridz"]))]
+    if "ivs" in p:
+        lines += [f"ivs {p['ivs']}", f"vpvs {p['vpvs']}"]
     return "\n".join(lines) + "\n"
 
 
@@ -234,4 +235,4 @@ def load_golden(seed):
     return p, outs
 
 
-SEEDS = (1, 2, 3, 4)
+SEEDS = (1, 2, 3, 4, 5, 6)

@@ -15,6 +15,8 @@ def gpu_grid(lib, p):
     g = lib.loc_grid_from_spec(p["nx"], p["ny"], p["nz"], p["x0"], p["y0"], p["z0"], p["h"])
     g.kmin, g.ndiv, g.ndiv2 = p["kmin"], p["ndiv"], p["ndiv2"]
     g.nthres, g.resthres, g.resthrep, g.stdmax = p["nthres"], p["resthres"], p["resthrep"], p["stdmax"]
+    if "ivs" in p:
+        g.ivs, g.vpvs = p["ivs"], p["vpvs"]
     return g
 
 
