@@ -27,6 +27,7 @@
 #include <stdint.h>
 
 #include "fd_face_table.h"
+#include "fdgpu_check.cuh"
 #include "fdgpu_layout.h"
 
 namespace fdk {
@@ -101,6 +102,7 @@ struct PointCtx {
 
 __device__ __forceinline__ const double *node_row(const fd_geo_dev &g, int z, int y)
 {
+    if (!FD_OK(z, g.nz, 1) || !FD_OK(y, g.ny, 2)) { z = 0; y = 0; }
     return g.node + ((long long)z * g.ny + y) * FD_N_N;
 }
 

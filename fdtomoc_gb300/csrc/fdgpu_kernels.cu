@@ -807,7 +807,8 @@ __device__ unsigned key_event(const fd_station_dev &sd, Shared &sh, int I, int j
     for (int k = 0; k < 8; k++) {
         int du, dv;
         nb_off(k, du, dv);
-        tn[k] = ((inr >> k) & 1u) ? vload(sd.T[qin + du * su + dv * sv]) : 0.f;
+        const long long qk = qin + du * su + dv * sv;
+        tn[k] = (((inr >> k) & 1u) && FD_OK(qk, (long long)sd.g.nx * sd.g.ny * sd.g.nz, 12)) ? vload(sd.T[qk]) : 0.f;
     }
     const unsigned long long kj = node_key(vload(sd.T[qin]), j);
     unsigned em = 0;
@@ -817,6 +818,9 @@ __device__ unsigned key_event(const fd_station_dev &sd, Shared &sh, int I, int j
         nb_off(k, du, dv);
         if (((inr >> k) & 1u) && node_key(tn[k], j + du + dv * r.nuf) < kj) em |= 1u << k;
     }
+    if (!FD_OK(q, (long long)sd.g.nx * sd.g.ny * sd.g.nz, 13) || !FD_OK(qin, (long long)sd.g.nx * sd.g.ny * sd.g.nz, 29)
+        || !FD_OK(I, sd.scr.ginst_cap, 14))
+        return 0u;
     sd.scr.gemask[q] = (unsigned char)em;
     wfence(sh);
     const unsigned lat = (unsigned)__popc(inr & ~em);
@@ -838,6 +842,7 @@ __device__ __forceinline__ void graph_dec(const fd_station_dev &sd, Shared &sh, 
                                           const int qxyz[3], bool inner)
 {
     const unsigned dec = inner ? 1u : (1u << 16);
+    if (!FD_OK(q, (long long)sd.g.nx * sd.g.ny * sd.g.nz, 19)) return;
     const unsigned nw = atomicSub(&sd.scr.gcnt[q], dec) - dec;
     if (inner && (nw & 0xFFu) == 0u) {
         /* q's inner block is complete: its key and in-face order are now known */
@@ -852,6 +857,7 @@ __device__ void graph_release(const fd_station_dev &sd, Shared &sh, int F, long 
                               bool writer, float st0, float st4, float tin)
 {
     const GraphSmem &gs = gsmem(sh);
+    if (!FD_OK(p, (long long)sd.g.nx * sd.g.ny * sd.g.nz, 15) || !FD_OK(I, sd.scr.ginst_cap, 16)) return;
     const GRect &r = gs.rect[I];
     fd_ginst &gi = sd.scr.ginst[I];
     /* records: of every point when a point may need an earlier one's; else only the last instance's,
@@ -921,6 +927,7 @@ __device__ void graph_release(const fd_station_dev &sd, Shared &sh, int F, long 
         int du, dv;
         nb_off(k, du, dv);
         const long long q = p + du * t_stride(sd, fr.axis_u) + dv * t_stride(sd, fr.axis_v);
+        if (!FD_OK(q, (long long)sd.g.nx * sd.g.ny * sd.g.nz, 17)) continue;
         const unsigned nw = atomicSub(&sd.scr.gcnt[q], 1u << 8) - (1u << 8);
         if (ready_word(nw)) graph_ready(sd, sh, F, q);
     }
@@ -1025,7 +1032,7 @@ __device__ bool commit_node(const fd_station_dev &sd, Shared &sh, const TrialDes
         }
     }
     if (permissive && win2d) return false;
-    if (lt(guess, told)) {
+    if (lt(guess, told) && FD_OK(wh.p, (long long)sd.g.nx * sd.g.ny * sd.g.nz, 11)) {
         sd.T[wh.p] = __double2float_rn(guess);
         if (lastK >= 0) {
             /* only the last head trial that lowered the minimum sets the measure that is tested */
@@ -1117,9 +1124,12 @@ __device__ void warp_chunk(const fd_station_dev &sd, Shared &sh, const CtaSmem &
             if (uu >= 0 && uu < wh.r.nu && vv >= 0 && vv < wh.r.nv) {
                 /* with several CTAs, through L2: another SM may have written it since this SM last
                  * read it; one CTA's own stores keep its L1 current */
-                const float *pt = &sd.T[wh.p + du * su + dv * sv + (w ? inner_t : 0ll)];
-                tv = sh.cs > 1 ? __ldcg(pt) : *pt;
-                svv = __ldg(&sd.S[pS + du * ssu + dv * ssv + (w ? inner_s : 0ll)]);
+                const long long it = wh.p + du * su + dv * sv + (w ? inner_t : 0ll);
+                if (FD_OK(it, (long long)sd.g.nx * sd.g.ny * sd.g.nz, 27)) {
+                    const float *pt = &sd.T[it];
+                    tv = sh.cs > 1 ? __ldcg(pt) : *pt;
+                    svv = __ldg(&sd.S[pS + du * ssu + dv * ssv + (w ? inner_s : 0ll)]);
+                }
             }
             tr[nb] = tv;
             sr[nb] = svv;
@@ -1260,6 +1270,7 @@ __device__ void resume_graph(const fd_station_dev &sd, Shared &sh, const CtaSmem
     const int lane = threadIdx.x & 31;
     const GraphSmem &gs = gsmem(sh);
     const int nx = sd.g.nx, ny = sd.g.ny;
+    if (!FD_OK(w, (long long)sd.g.nx * sd.g.ny * sd.g.nz, 20)) return;
     const int wxy = w / nx;
     const int xyz[3] = {w - wxy * nx, wxy % ny, wxy / ny};
     const int ow = owner_of(gs, sh.gfaces, xyz[0], xyz[1], xyz[2]);
@@ -1288,7 +1299,9 @@ __device__ void resume_graph(const fd_station_dev &sd, Shared &sh, const CtaSmem
         if (lane == 0) {
             if (best) {
                 const long long p = inst_node(sd, r, (int)(best & 0xffffffffu));
-                if (!(vload(sd.scr.gcnt[p]) & FD_DONEB) && wait_point(sd, sh, w, p)) {
+                if (!FD_OK((long long)(best & 0xffffffffu), n, 21)) {
+                    verdict = 2;
+                } else if (!(vload(sd.scr.gcnt[p]) & FD_DONEB) && wait_point(sd, sh, w, p)) {
                     verdict = 2;
                 } else {
                     wfence(sh);
@@ -1305,6 +1318,7 @@ __device__ void resume_graph(const fd_station_dev &sd, Shared &sh, const CtaSmem
                     const unsigned long long ek = vload(sd.scr.ginst[J].exitkey);
                     if (ek) {
                         const long long p = inst_node(sd, rj, (int)(ek & 0xffffffffu));
+                        if (!FD_OK((long long)(ek & 0xffffffffu), rect_n(rj), 22)) break;
                         t0 = vload(sd.scr.grec[p].x);
                         t4 = vload(sd.scr.grec[p].y);
                         break;
@@ -1432,6 +1446,13 @@ __device__ void run_walk(const fd_station_dev &sd, Shared &sh, const CtaSmem &cs
                     e = *q;
                 }
                 if (e < 0) atomicCAS(&sh.w->status, 0, 9);   /* a claimed entry never written */
+                /* an entry outside the walk's nodes ends the walk with a status instead of an access */
+                const long long bound = sh.graph ? (long long)sd.g.nx * sd.g.ny * sd.g.nz : (long long)sh.n;
+                if (e >= bound) {
+                    (void)FD_OK(e, bound, 23);
+                    atomicCAS(&sh.w->status, 0, 18);
+                    e = -1;
+                }
             }
             wfence(sh);
             warp_chunk(sd, sh, cs, ws, sh.graph ? qf : sh.face, e, false, 0.f, 0.f, dag, cn);
@@ -1440,6 +1461,12 @@ __device__ void run_walk(const fd_station_dev &sd, Shared &sh, const CtaSmem &cs
         }
         if (act == 2) {
             wfence(sh);
+            const long long bound = sh.graph ? (long long)sd.g.nx * sd.g.ny * sd.g.nz : (long long)sh.n;
+            if (h >= bound) {
+                (void)FD_OK(h, bound, 24);
+                if (lane == 0) atomicCAS(&sh.w->status, 0, 18);
+                h = -1;
+            }
             if (h >= 0) {
                 if (sh.graph)
                     resume_graph(sd, sh, cs, ws, h, cn);
@@ -1660,6 +1687,7 @@ __device__ void graph_sweep(const fd_station_dev &sd, Shared &sh, CtaSmem &cs, W
             const bool prev = sh.single && I > 0 && gs.rect[I - 1].layer == r.layer + fr.inner;
             for (int j = gt; j < n; j += gstride) {
                 const long long p = inst_node(sd, r, j);
+                if (!FD_OK(p, (long long)nx * ny * nz, 25)) continue;
                 unsigned cin = 0, c2 = 0, cx = 0;
                 if (sh.single) {
                     /* one face: the same-instance neighbours and the previous plane's inner block */
@@ -1718,7 +1746,7 @@ __device__ void graph_sweep(const fd_station_dev &sd, Shared &sh, CtaSmem &cs, W
         /* the stencil state after the sweep: the record of its last writer */
         for (int I = ninst - 1; I >= 0; I--) {
             const unsigned long long ek = vload(sd.scr.ginst[I].exitkey);
-            if (ek) {
+            if (ek && FD_OK((long long)(ek & 0xffffffffu), rect_n(gs.rect[I]), 26)) {
                 const float2 r = __ldcg(&sd.scr.grec[inst_node(sd, gs.rect[I], (int)(ek & 0xffffffffu))]);
                 sh.carry_t0 = r.x;
                 sh.carry_t4 = r.y;
@@ -2132,6 +2160,19 @@ extern "C" long long fdk_serve_smem_bytes(void)
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     return optin - (long long)dyn_smem_limit_margin();
 }
+
+#ifdef FD_SELFCHECK
+/* the index-check record of FD_SELFCHECK builds: count, first site, first index; cleared after reading */
+extern "C" cudaError_t fdk_selfcheck_read(unsigned long long *out)
+{
+    cudaError_t e = cudaMemcpyFromSymbol(out, fd_selfcheck_words, sizeof(unsigned long long) * 3);
+    if (e == cudaSuccess) {
+        const unsigned long long z[3] = {0, 0, 0};
+        e = cudaMemcpyToSymbol(fd_selfcheck_words, z, sizeof z);
+    }
+    return e;
+}
+#endif
 
 /* slowness = 1/velocity, float division as the reference does it (src/sphfd.c:689-690) */
 __global__ void fd_v2s(const float *v, float *s, long long n)

@@ -145,6 +145,7 @@ __device__ __forceinline__ void dist_rt(const fd_geo_dev &g, int cls, int z, int
         d = g.h;
         inv = g.inv_h;
     } else if (cls == CH_RDQ) {
+        if (!FD_OK(z, g.nz, 3)) z = 0;
         const double *zr = g.zrow + (long long)z * FD_Z_N;
         d = zr[FD_Z_RDQ];
         inv = zr[FD_Z_INV_RDQ];
@@ -169,8 +170,8 @@ __device__ __forceinline__ double factor_rt(const fd_geo_dev &g, int kind, int z
     case FK_H: return g.h;
     case FK_DQ: return g.dq;
     case FK_DF: return g.df;
-    case FK_R: return g.zrow[(long long)z * FD_Z_N + FD_Z_R];
-    case FK_S: return g.ysin[y];
+    case FK_R: return g.zrow[(long long)(FD_OK(z, g.nz, 4) ? z : 0) * FD_Z_N + FD_Z_R];
+    case FK_S: return g.ysin[FD_OK(y, g.ny, 5) ? y : 0];
     default: return f2d(slow);
     }
 }
@@ -197,7 +198,9 @@ __device__ __forceinline__ double eval_3d(const TrialDesc &d, const float *t18, 
     sum = sum + f2d(s18[NB_POINT]);
     const double slo = scale2k<-3>(sum);
     const double sl16 = scale2k<1>(sum) * slo;
-    const double *C = g.cell + ((long long)(z + d.zmin) * (g.ny - 1) + (y + d.ymin)) * FD_C_N;
+    int zc = z + d.zmin, yc = y + d.ymin;
+    if (!FD_OK(zc, g.nz - 1, 6) || !FD_OK(yc, g.ny - 1, 7)) { zc = 0; yc = 0; }
+    const double *C = g.cell + ((long long)zc * (g.ny - 1) + yc) * FD_C_N;
     const double a = C[d.a_idx], i2a = C[d.i2a_idx];
     double b = t[0] * C[d.prow[0]];
 #pragma unroll

@@ -85,7 +85,8 @@ typedef struct {
     int32_t detail;           /* on FDGPU_ESCHED, the check that failed: 3 nodes left that nothing
                                  releases, 4 sweep bound, 6 a pipelined sweep met a point needing an
                                  earlier point's stencil state, 8 a worker waited too long, 9 a
-                                 claimed queue entry was never written, 10 a node queued twice */
+                                 claimed queue entry was never written, 10 a node queued twice,
+                                 18 a queue entry outside the walk's nodes */
     int32_t sm;               /* the SM whose CTA ran the solve */
     int32_t pad;
 } fdgpu_stats;
