@@ -30,6 +30,10 @@ extern "C" cudaError_t fdk_launch_geo_build(int nx, int ny, int nz, double h, do
 extern "C" cudaError_t fdk_launch_solve(const fd_station_dev *stations, int nst, long long max_face_pad, int cluster,
                                         cudaStream_t stream);
 extern "C" cudaError_t fdk_launch_v2s(const float *v, float *s, long long n, cudaStream_t stream);
+extern "C" cudaError_t fdk_solve_config(int nst, long long max_face_pad, int cluster, long long *bytes_out,
+                                        int *csz_out);
+extern "C" cudaError_t fdk_solve_launch(const fd_station_dev *stations, int nst, long long bytes, int cs,
+                                        cudaStream_t stream);
 extern "C" cudaError_t fdk_probe_fp64(double *scratch, int blocks, int threads, int iters, float *ms, cudaStream_t s);
 
 namespace {
@@ -67,6 +71,11 @@ struct Geo {
 
 using GeoKey = std::tuple<int, int, uint64_t, uint64_t, uint64_t, uint64_t, uint64_t>;
 
+/* Device buffers of one prepared batch: scratch, station records, statistics, box trig tables. */
+struct BatchBufs {
+    DevBuf scratch, stations, stats, trig;
+};
+
 uint64_t bits(double x)
 {
     uint64_t b;
@@ -81,7 +90,8 @@ struct fdgpu_ctx {
     int cluster = 0;   /* CTAs per station: 0 automatic */
     cudaStream_t stream = nullptr;
     std::map<GeoKey, std::unique_ptr<Geo>> geos;
-    DevBuf scratch, stations, stats, trig, model, fields;
+    BatchBufs batch;   /* the buffers of fdgpu_solve_device, kept for the next call */
+    DevBuf model, fields;
     std::string err;
 };
 
@@ -239,14 +249,14 @@ extern "C" int fdgpu_set_cluster(fdgpu_ctx *ctx, int ctas_per_station)
     return FDGPU_OK;
 }
 
-extern "C" int fdgpu_solve_device(fdgpu_ctx *ctx, int n, const fdgpu_station *st, const float *slowness,
-                                  long long s_sy, long long s_sz, float *const *d_times, int times_initialised,
-                                  fdgpu_stats *stats, void *stream)
+namespace {
+
+/* Check the stations and lay out their records in bufs (queued on cs): everything a launch of
+ * fd_solve reads, except the fields and the slowness it points at.  *max_pad: the largest face. */
+int prepare_batch(fdgpu_ctx *ctx, int n, const fdgpu_station *st, const float *slowness, long long s_sy,
+                  long long s_sz, float *const *d_times, int times_initialised, BatchBufs &bufs, cudaStream_t cs,
+                  long long *max_pad_out)
 {
-    if (!ctx || n < 0 || (n > 0 && (!st || !slowness || !d_times))) return FDGPU_EINVAL;
-    if (n == 0) return FDGPU_OK;
-    FD_CU(ctx, cudaSetDevice(ctx->device));
-    cudaStream_t cs = stream ? (cudaStream_t)stream : ctx->stream;
     if (((uintptr_t)slowness & 3u) != 0) return FDGPU_EINVAL;
     for (int k = 0; k < n; k++) {
         const int c = check_station(st[k]);
@@ -257,12 +267,12 @@ extern "C" int fdgpu_solve_device(fdgpu_ctx *ctx, int n, const fdgpu_station *st
     /* scratch and per-station records: per station, face scratch, then the sweep-graph arrays */
     std::vector<size_t> off(n + 1, 0);
     for (int k = 0; k < n; k++) off[k + 1] = off[k] + fdh::face_bytes(st[k]) + fdh::graph_bytes(st[k]);
-    FD_CU(ctx, ctx->scratch.ensure(off[n]));
-    FD_CU(ctx, ctx->stations.ensure(sizeof(fd_station_dev) * n));
-    FD_CU(ctx, ctx->stats.ensure(sizeof(fd_station_stats) * n));
+    FD_CU(ctx, bufs.scratch.ensure(off[n]));
+    FD_CU(ctx, bufs.stations.ensure(sizeof(fd_station_dev) * n));
+    FD_CU(ctx, bufs.stats.ensure(sizeof(fd_station_stats) * n));
     int maxt = 0;
     for (int k = 0; k < n; k++) maxt = std::max(maxt, fdh::box_trig_count(st[k]));
-    FD_CU(ctx, ctx->trig.ensure(sizeof(double) * (size_t)maxt * n + 8));
+    FD_CU(ctx, bufs.trig.ensure(sizeof(double) * (size_t)maxt * n + 8));
     std::vector<fd_station_dev> hs(n);
     long long max_pad = 16;
     std::vector<double> trig((size_t)maxt * n, 0.0);
@@ -273,10 +283,10 @@ extern "C" int fdgpu_solve_device(fdgpu_ctx *ctx, int n, const fdgpu_station *st
         if (!g) return status;
         const fdh::GeoPtrs gp{g->ysin.as<double>(), g->zrow.as<double>(), g->node.as<double>(), g->cell.as<double>()};
         fdh::box_trig(s, trig.data() + (size_t)maxt * k);
-        char *base = ctx->scratch.as<char>() + off[k];
+        char *base = bufs.scratch.as<char>() + off[k];
         fdh::fill_station(hs[k], s, gp, d_times[k], slowness, s_sy, s_sz,
                           (s.srctype == 1 && !times_initialised) ? 0 : 1, base, base + fdh::face_bytes(s),
-                          ctx->trig.as<double>() + (size_t)maxt * k, ctx->stats.as<fd_station_stats>() + k);
+                          bufs.trig.as<double>() + (size_t)maxt * k, bufs.stats.as<fd_station_stats>() + k);
         max_pad = std::max(max_pad, hs[k].max_face_pad);
     }
     /* Launch order: largest grids first.  CTA i solves record i, and CTAs beyond the resident ones
@@ -286,11 +296,19 @@ extern "C" int fdgpu_solve_device(fdgpu_ctx *ctx, int n, const fdgpu_station *st
     std::stable_sort(hs.begin(), hs.end(), [](const fd_station_dev &a, const fd_station_dev &b) {
         return (long long)a.g.nx * a.g.ny * a.g.nz > (long long)b.g.nx * b.g.ny * b.g.nz;
     });
-    FD_CU(ctx, cudaMemcpyAsync(ctx->trig.p, trig.data(), sizeof(double) * trig.size(), cudaMemcpyHostToDevice, cs));
-    FD_CU(ctx, cudaMemcpyAsync(ctx->stations.p, hs.data(), sizeof(fd_station_dev) * n, cudaMemcpyHostToDevice, cs));
-    FD_CU(ctx, fdk_launch_solve(ctx->stations.as<fd_station_dev>(), n, max_pad, ctx->cluster, cs));
+    FD_CU(ctx, cudaMemcpyAsync(bufs.trig.p, trig.data(), sizeof(double) * trig.size(), cudaMemcpyHostToDevice, cs));
+    FD_CU(ctx, cudaMemcpyAsync(bufs.stations.p, hs.data(), sizeof(fd_station_dev) * n, cudaMemcpyHostToDevice, cs));
+    /* the host vectors go away on return: the copies must have left them */
+    FD_CU(ctx, cudaStreamSynchronize(cs));
+    *max_pad_out = max_pad;
+    return FDGPU_OK;
+}
+
+/* the public statistics of n solves from their device records (queued on cs, then waited for) */
+int read_stats(fdgpu_ctx *ctx, const DevBuf &stats_buf, int n, fdgpu_stats *stats, cudaStream_t cs)
+{
     std::vector<fd_station_stats> hst(n);
-    FD_CU(ctx, cudaMemcpyAsync(hst.data(), ctx->stats.p, sizeof(fd_station_stats) * n, cudaMemcpyDeviceToHost, cs));
+    FD_CU(ctx, cudaMemcpyAsync(hst.data(), stats_buf.p, sizeof(fd_station_stats) * n, cudaMemcpyDeviceToHost, cs));
     FD_CU(ctx, cudaStreamSynchronize(cs));
     int rc = FDGPU_OK;
     for (int k = 0; k < n; k++) {
@@ -298,6 +316,84 @@ extern "C" int fdgpu_solve_device(fdgpu_ctx *ctx, int n, const fdgpu_station *st
         if (hst[k].status && rc == FDGPU_OK) rc = FDGPU_ESCHED;
     }
     return rc;
+}
+
+}  // namespace
+
+struct fdgpu_batch {
+    fdgpu_ctx *ctx = nullptr;
+    int n = 0;
+    long long max_pad = 16;
+    long long smem_bytes = 0;   /* launch shape, fixed at creation */
+    int csz = 1;
+    BatchBufs bufs;
+};
+
+extern "C" int fdgpu_solve_device(fdgpu_ctx *ctx, int n, const fdgpu_station *st, const float *slowness,
+                                  long long s_sy, long long s_sz, float *const *d_times, int times_initialised,
+                                  fdgpu_stats *stats, void *stream)
+{
+    if (!ctx || n < 0 || (n > 0 && (!st || !slowness || !d_times))) return FDGPU_EINVAL;
+    if (n == 0) return FDGPU_OK;
+    FD_CU(ctx, cudaSetDevice(ctx->device));
+    cudaStream_t cs = stream ? (cudaStream_t)stream : ctx->stream;
+    BatchBufs &bufs = ctx->batch;
+    long long max_pad = 16;
+    int rc = prepare_batch(ctx, n, st, slowness, s_sy, s_sz, d_times, times_initialised, bufs, cs, &max_pad);
+    if (rc == FDGPU_OK) {
+        const cudaError_t e = fdk_launch_solve(bufs.stations.as<fd_station_dev>(), n, max_pad, ctx->cluster, cs);
+        rc = e ? cuda_fail(ctx, e, "fdk_launch_solve") : read_stats(ctx, bufs.stats, n, stats, cs);
+    }
+    return rc;
+}
+
+extern "C" int fdgpu_batch_create(fdgpu_ctx *ctx, int n, const fdgpu_station *st, const float *slowness,
+                                  long long s_sy, long long s_sz, float *const *d_times, int times_initialised,
+                                  fdgpu_batch **out)
+{
+    if (!out) return FDGPU_EINVAL;
+    *out = nullptr;
+    if (!ctx || n < 1 || !st || !slowness || !d_times) return FDGPU_EINVAL;
+    FD_CU(ctx, cudaSetDevice(ctx->device));
+    auto *b = new (std::nothrow) fdgpu_batch;
+    if (!b) return FDGPU_ENOMEM;
+    b->ctx = ctx;
+    b->n = n;
+    int rc = prepare_batch(ctx, n, st, slowness, s_sy, s_sz, d_times, times_initialised, b->bufs, ctx->stream,
+                           &b->max_pad);
+    if (!rc) {
+        const cudaError_t e = fdk_solve_config(n, b->max_pad, ctx->cluster, &b->smem_bytes, &b->csz);
+        if (e) rc = cuda_fail(ctx, e, "fdk_solve_config");
+    }
+    if (rc) {
+        delete b;
+        return rc;
+    }
+    *out = b;
+    return FDGPU_OK;
+}
+
+extern "C" int fdgpu_batch_run(fdgpu_batch *b, void *stream)
+{
+    if (!b) return FDGPU_EINVAL;
+    fdgpu_ctx *ctx = b->ctx;
+    cudaStream_t cs = stream ? (cudaStream_t)stream : ctx->stream;
+    FD_CU(ctx, fdk_solve_launch(b->bufs.stations.as<fd_station_dev>(), b->n, b->smem_bytes, b->csz, cs));
+    return FDGPU_OK;
+}
+
+extern "C" int fdgpu_batch_stats(fdgpu_batch *b, fdgpu_stats *stats, void *stream)
+{
+    if (!b) return FDGPU_EINVAL;
+    fdgpu_ctx *ctx = b->ctx;
+    return read_stats(ctx, b->bufs.stats, b->n, stats, stream ? (cudaStream_t)stream : ctx->stream);
+}
+
+extern "C" void fdgpu_batch_destroy(fdgpu_batch *b)
+{
+    if (!b) return;
+    cudaSetDevice(b->ctx->device);
+    delete b;   /* frees its device buffers */
 }
 
 extern "C" int fdgpu_solve_host(fdgpu_ctx *ctx, int n, const fdgpu_station *st, const float *velocity, int mnx,

@@ -2078,12 +2078,12 @@ static size_t dyn_smem_limit_margin()
 /* cluster: CTAs per station; 0 picks more than one when the stations alone would leave SMs idle,
  * up to 8 (1 keeps every station on one CTA).  Reduced until every cluster of the launch is
  * co-resident. */
-extern "C" cudaError_t fdk_launch_solve(const fd_station_dev *stations, int nst, long long max_face_pad, int cluster,
-                                        cudaStream_t stream)
+/* Launch shape of a batch: dynamic shared memory (the warp areas, plus the sweep-graph tables or the
+ * face's dependency bytes, whichever is larger and fits) and CTAs per station; sets the kernel's
+ * shared-memory limit.  Host calls only (no stream work): done once per batch, outside any capture. */
+extern "C" cudaError_t fdk_solve_config(int nst, long long max_face_pad, int cluster, long long *bytes_out,
+                                        int *csz_out)
 {
-    if (nst <= 0) return cudaSuccess;
-    /* dynamic shared memory: the warp areas, plus the sweep-graph tables or the face's dependency
-     * bytes, whichever is larger and fits */
     int dev = 0, optin = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
@@ -2112,6 +2112,17 @@ extern "C" cudaError_t fdk_launch_solve(const fd_station_dev *stations, int nst,
     while (cs > 1 && !fits(cs)) cs /= 2;
     if (cs > FD_MAX_CLUSTER) cs = FD_MAX_CLUSTER;
     if (bytes - base < graph) cs = 1;   /* no room for the sweep-graph tables: face walks, one CTA */
+    *bytes_out = bytes;
+    *csz_out = cs;
+    return cudaSuccess;
+}
+
+/* One launch of a configured batch: queues the kernel only (capturable in a CUDA graph). */
+extern "C" cudaError_t fdk_solve_launch(const fd_station_dev *stations, int nst, long long bytes, int cs,
+                                        cudaStream_t stream)
+{
+    if (nst <= 0) return cudaSuccess;
+    const long long base = (long long)fdk::kSmemBase;
     if (cs == 1) {
         fdk::fd_solve<<<nst, FD_BLOCK, (size_t)bytes, stream>>>(stations, nst, (int)(bytes - base), 1, nullptr, 0);
         return cudaGetLastError();
@@ -2128,9 +2139,19 @@ extern "C" cudaError_t fdk_launch_solve(const fd_station_dev *stations, int nst,
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    e = cudaLaunchKernelEx(&cfg, fdk::fd_solve, stations, nst, (int)(bytes - base), cs,
-                           static_cast<const fd_serve_queue *>(nullptr), 0);
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, fdk::fd_solve, stations, nst, (int)(bytes - base), cs,
+                                             static_cast<const fd_serve_queue *>(nullptr), 0);
     return e == cudaSuccess ? cudaGetLastError() : e;
+}
+
+extern "C" cudaError_t fdk_launch_solve(const fd_station_dev *stations, int nst, long long max_face_pad, int cluster,
+                                        cudaStream_t stream)
+{
+    if (nst <= 0) return cudaSuccess;
+    long long bytes = 0;
+    int cs = 1;
+    const cudaError_t e = fdk_solve_config(nst, max_face_pad, cluster, &bytes, &cs);
+    return e != cudaSuccess ? e : fdk_solve_launch(stations, nst, bytes, cs, stream);
 }
 
 /* The long-running grid of a serving session: nctas CTAs (one per SM), numbered cta_id0 onward in

@@ -149,6 +149,12 @@ def load() -> C.CDLL:
         lib.fdgpu_solve_device.argtypes = [P, C.c_int, C.POINTER(Station), C.c_void_p, C.c_longlong, C.c_longlong,
                                            C.POINTER(C.c_void_p), C.c_int, C.POINTER(Stats), C.c_void_p]
         lib.fdgpu_probe_fp64.argtypes = [P, C.POINTER(C.c_double)]
+        lib.fdgpu_batch_create.argtypes = [P, C.c_int, C.POINTER(Station), C.c_void_p, C.c_longlong, C.c_longlong,
+                                           C.POINTER(C.c_void_p), C.c_int, C.POINTER(P)]
+        lib.fdgpu_batch_run.argtypes = [P, C.c_void_p]
+        lib.fdgpu_batch_stats.argtypes = [P, C.POINTER(Stats), C.c_void_p]
+        lib.fdgpu_batch_destroy.argtypes = [P]
+        lib.fdgpu_batch_destroy.restype = None
         lib.fdgpu_velocity_to_slowness.argtypes = [P, C.c_void_p, C.c_void_p, C.c_longlong, C.c_void_p]
         lib.fdgpu_sphfd.argtypes = [C.c_int, C.POINTER(C.c_char_p), C.c_char_p]
         lib.fdgpu_sphfd_parlist.argtypes = [C.c_int, C.POINTER(C.c_char_p), C.c_char_p, C.POINTER(C.c_int)]
@@ -271,6 +277,40 @@ class Context:
     def velocity_to_slowness(self, vel_ptr: int, slow_ptr: int, n: int, stream_ptr: int = 0):
         _check(self.lib.fdgpu_velocity_to_slowness(self.ptr, C.c_void_p(vel_ptr), C.c_void_p(slow_ptr), n,
                                                    C.c_void_p(stream_ptr)), self.ptr)
+
+
+class Batch:
+    """fdgpu_batch: stations prepared once, launched many times (capturable in a CUDA graph)."""
+
+    def __init__(self, ctx: "Context", stations, slowness_ptr: int, s_sy: int, s_sz: int, time_ptrs,
+                 initialised=False):
+        self.lib = load()
+        self.ctx = ctx
+        self.n = len(stations)
+        arr = (Station * self.n)(*stations)
+        tp = (C.c_void_p * self.n)(*time_ptrs)
+        self.ptr = C.c_void_p()
+        _check(self.lib.fdgpu_batch_create(ctx.ptr, self.n, arr, C.c_void_p(slowness_ptr), s_sy, s_sz, tp,
+                                           1 if initialised else 0, C.byref(self.ptr)), ctx.ptr)
+
+    def run(self, stream_ptr: int = 0):
+        _check(self.lib.fdgpu_batch_run(self.ptr, C.c_void_p(stream_ptr)), self.ctx.ptr)
+
+    def stats(self, stream_ptr: int = 0):
+        st = (Stats * self.n)()
+        _check(self.lib.fdgpu_batch_stats(self.ptr, st, C.c_void_p(stream_ptr)), self.ctx.ptr)
+        return [s.as_dict() for s in st]
+
+    def close(self):
+        if self.ptr:
+            self.lib.fdgpu_batch_destroy(self.ptr)
+            self.ptr = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def loc_grid_from_spec(nx, ny, nz, x0_deg, y0_deg, z0_km, h_km) -> LocGrid:

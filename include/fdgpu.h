@@ -124,6 +124,20 @@ int fdgpu_solve_device(fdgpu_ctx *ctx, int n, const fdgpu_station *st, const flo
                        long long s_sz, float *const *d_times, int times_initialised, fdgpu_stats *stats,
                        void *stream);
 
+/* The same batch prepared once and launched many times, e.g. inside a captured CUDA graph: create
+ * builds the geometry tables, the scratch and the station records on the device (the context must
+ * outlive the batch); run queues the solve of all n stations as one kernel launch on `stream` (NULL:
+ * the context's), with no allocation and no host synchronisation, so it can be captured; stats waits
+ * for `stream` and reads the statistics of the last run.  Point-source stations initialise their
+ * fields in every run; stations that start from a supplied field (times_initialised) need it put
+ * back before each run.  Runs of one batch share its scratch: two of them must not overlap. */
+typedef struct fdgpu_batch fdgpu_batch;
+int fdgpu_batch_create(fdgpu_ctx *ctx, int n, const fdgpu_station *st, const float *slowness, long long s_sy,
+                       long long s_sz, float *const *d_times, int times_initialised, fdgpu_batch **out);
+int fdgpu_batch_run(fdgpu_batch *batch, void *stream);
+int fdgpu_batch_stats(fdgpu_batch *batch, fdgpu_stats *stats, void *stream);
+void fdgpu_batch_destroy(fdgpu_batch *batch);
+
 /* velocity -> slowness on the device, slow[i] = 1/v[i] as the reference rounds it (src/sphfd.c:689) */
 int fdgpu_velocity_to_slowness(fdgpu_ctx *ctx, const float *d_velocity, float *d_slowness, long long n,
                                void *stream);

@@ -1,6 +1,8 @@
-"""Batched solves equal solo solves: stations of different sizes and sources solved in one batch
-(packed back to back in one device buffer by the host entry point) give the same fields, bit for
-bit, as each station solved alone."""
+"""fdgpu_batch_*: stations prepared once (checks, geometry, records, stats slots), then launched as
+often as the caller wants, each launch a single kernel on the caller's stream.  A launch queues no
+host work, so it can be captured in a CUDA graph; every replay must give the fields that
+fdgpu_solve_device gives for the same stations, bit for bit.
+"""
 import numpy as np
 import pytest
 
@@ -9,72 +11,117 @@ from cases import random_case, write_random_case
 pytestmark = pytest.mark.gpu
 
 
-def test_batch_equals_alone(gpu_lib, tmp_path):
-    lib = gpu_lib
-    # windows of one model: different sizes (odd lengths), origins and sources
-    model = random_case(101)["vel"]
-    nz, ny, nx = model.shape
-    stations, solo = [], []
-    for k, seed in enumerate([3, 8, 11, 21]):
-        c = random_case(seed)
-        pf = write_random_case(c, str(tmp_path / f"c{k}"))
+def _cases(lib, tmp_path, seeds):
+    out = []
+    for s in seeds:
+        c = random_case(s)
+        pf = write_random_case(c, str(tmp_path / f"c{s}"))
         st, _, _ = lib.station_from_par("par=" + pf)
-        stations.append((st, c["vel"]))
+        if st.srctype == 1:
+            out.append((st, c["vel"]))
+    return out
+
+
+def _slowness(ctx, vel):
+    import torch
+    v = torch.from_numpy(np.ascontiguousarray(vel).reshape(-1)).cuda()
+    slow = torch.empty_like(v)
+    ctx.velocity_to_slowness(v.data_ptr(), slow.data_ptr(), v.numel())
+    return slow
+
+
+def test_batch_replayed_from_a_cuda_graph(gpu_lib, tmp_path):
+    import torch
+    lib = gpu_lib
+    cases = _cases(lib, tmp_path, range(1, 40))[:6]
+    assert len(cases) >= 3
     with lib.Context(0) as ctx:
-        for st, vel in stations:
-            (t,), _ = ctx.solve_host([st], vel)
-            solo.append(t)
-        # the same stations in one batch: each reads its own model, so batch those sharing a model
-        # layout by stacking them into one model grid along z is not possible; instead batch the
-        # first station's model with windows of itself
-        st0, vel0 = stations[0]
-        wins = []
-        for (ox, oy, oz) in [(0, 0, 0), (1, 0, 0), (0, 1, 1)]:
-            w = lib.Station.from_buffer_copy(st0)
-            w.nx, w.ny, w.nz = st0.nx - ox, st0.ny - oy, st0.nz - oz
-            w.ox, w.oy, w.oz = ox, oy, oz
-            w.xs = min(w.xs, w.nx - 1)
-            w.ys = min(w.ys, w.ny - 1)
-            w.zs = min(w.zs, w.nz - 1)
-            wins.append(w)
-        batch, stats = ctx.solve_host(wins, vel0)
-        for w, b in zip(wins, batch):
-            v = np.ascontiguousarray(vel0[w.oz:w.oz + w.nz, w.oy:w.oy + w.ny, w.ox:w.ox + w.nx])
-            w2 = lib.Station.from_buffer_copy(w)
-            w2.ox = w2.oy = w2.oz = 0
-            (alone,), _ = ctx.solve_host([w2], v)
-            assert np.array_equal(alone.view(np.uint32), b.view(np.uint32))
-    assert all(s["status"] == 0 for s in stats)
+        for st, vel in cases:
+            nz, ny, nx = vel.shape
+            slow = _slowness(ctx, vel)
+            ref = torch.empty((st.nz, st.ny, st.nx), dtype=torch.float32, device="cuda")
+            ref_stats = ctx.solve_device([st], slow.data_ptr(), nx, nx * ny, [ref.data_ptr()])
+            torch.cuda.synchronize()
+
+            # the same station twice in one batch, each with its own field
+            outs = [torch.full_like(ref, -1.0) for _ in range(2)]
+            b = lib.Batch(ctx, [st, st], slow.data_ptr(), nx, nx * ny, [o.data_ptr() for o in outs])
+            s = torch.cuda.Stream()
+            s.wait_stream(torch.cuda.current_stream())
+            with torch.cuda.stream(s):
+                b.run(s.cuda_stream)                      # eager launch first
+            s.synchronize()
+            for o in outs:
+                assert torch.equal(o.view(torch.int32), ref.view(torch.int32))
+
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.stream(s):
+                with torch.cuda.graph(g, stream=s):
+                    b.run(s.cuda_stream)
+            for rep in range(2):
+                for o in outs:
+                    o.fill_(-1.0)
+                torch.cuda.synchronize()
+                g.replay()
+                torch.cuda.synchronize()
+                for k, o in enumerate(outs):
+                    assert torch.equal(o.view(torch.int32), ref.view(torch.int32)), f"replay {rep} field {k}"
+            stats = b.stats()
+            for x in stats:
+                assert x["status"] == 0
+                assert x["sweeps"] == ref_stats[0]["sweeps"]
+            b.close()
+            del g
 
 
-def test_multi_station_dropin(gpu_lib, tmp_path):
-    """Four par files sharing one velocity file run as one GPU batch through the drop-in parlist
-    entry point; each time file equals the oracle's."""
-    import os
-    from fdtomoc_gb300.formats import read_par, write_par
-    from oracle_util import run_oracle
-    c = random_case(4)
-    base = write_random_case(c, str(tmp_path / "m"))
-    par = read_par(base)
-    nx, ny, nz = int(par["nx"]), int(par["ny"]), int(par["nz"])
-    rng = np.random.default_rng(9)
-    pfs = []
-    for k in range(4):
-        q = dict(par)
-        q.pop("floatsrc", None)
-        for key in ("xs", "ys", "zs"):
-            q.pop(key, None)
-        q["floatsrc"] = 0
-        q["xs"], q["ys"], q["zs"] = int(rng.integers(0, nx)), int(rng.integers(0, ny)), int(rng.integers(0, nz))
-        q["timefile"] = f"s{k}.ptimes"
-        pf = str(tmp_path / f"s{k}.par")
-        write_par(pf, q)
-        pfs.append(pf)
-    os.makedirs(tmp_path / "gpu")
-    st = gpu_lib.sphfd_parlist(["par=" + p for p in pfs], str(tmp_path / "gpu"))
-    assert st == [0, 0, 0, 0]
-    for k, pf in enumerate(pfs):
-        run_oracle(pf, str(tmp_path / "orc"))
-        a = open(tmp_path / "orc" / f"s{k}.ptimes", "rb").read()
-        b = open(tmp_path / "gpu" / f"s{k}.ptimes", "rb").read()
-        assert a == b, f"station {k} differs"
+def test_graph_follows_a_model_updated_in_place(gpu_lib, tmp_path):
+    """The inversion loop: velocity -> slowness -> solve captured once; each iteration writes a new
+    velocity model into the same buffer and replays the graph."""
+    import torch
+    lib = gpu_lib
+    st, vel = _cases(lib, tmp_path, range(1, 40))[0]
+    nz, ny, nx = vel.shape
+    with lib.Context(0) as ctx:
+        v = torch.from_numpy(np.ascontiguousarray(vel).reshape(-1)).cuda()
+        slow = torch.empty_like(v)
+        out = torch.empty((st.nz, st.ny, st.nx), dtype=torch.float32, device="cuda")
+        ctx.velocity_to_slowness(v.data_ptr(), slow.data_ptr(), v.numel())
+        b = lib.Batch(ctx, [st], slow.data_ptr(), nx, nx * ny, [out.data_ptr()])
+        s = torch.cuda.Stream()
+        s.wait_stream(torch.cuda.current_stream())
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.stream(s):
+            with torch.cuda.graph(g, stream=s):
+                ctx.velocity_to_slowness(v.data_ptr(), slow.data_ptr(), v.numel(), s.cuda_stream)
+                b.run(s.cuda_stream)
+        rng = np.random.default_rng(7)
+        for it in range(3):
+            model = (vel * rng.uniform(0.9, 1.1, size=vel.shape)).astype(np.float32)
+            v.copy_(torch.from_numpy(model.reshape(-1)))
+            torch.cuda.synchronize()
+            g.replay()
+            torch.cuda.synchronize()
+            got = out.clone()
+            ref = torch.empty_like(out)
+            slow2 = torch.empty_like(v)
+            ctx.velocity_to_slowness(v.data_ptr(), slow2.data_ptr(), v.numel())
+            ctx.solve_device([st], slow2.data_ptr(), nx, nx * ny, [ref.data_ptr()])
+            torch.cuda.synchronize()
+            assert torch.equal(got.view(torch.int32), ref.view(torch.int32)), f"iteration {it}"
+        assert b.stats()[0]["status"] == 0
+        b.close()
+        del g
+
+
+def test_batch_rejects_bad_station(gpu_lib, tmp_path):
+    import torch
+    lib = gpu_lib
+    st, vel = _cases(lib, tmp_path, range(1, 40))[0]
+    with lib.Context(0) as ctx:
+        slow = _slowness(ctx, vel)
+        nz, ny, nx = vel.shape
+        bad = lib.Station.from_buffer_copy(st)
+        bad.nx = 0
+        out = torch.empty(16, dtype=torch.float32, device="cuda")
+        with pytest.raises(lib.FdgpuError):
+            lib.Batch(ctx, [bad], slow.data_ptr(), nx, nx * ny, [out.data_ptr()])
