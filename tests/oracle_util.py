@@ -147,3 +147,40 @@ def oracle_c2f(p, coarse):
     rc = lib.fdo_c2f(C.byref(g), src.ctypes.data_as(C.POINTER(C.c_float)), fine.ctypes.data_as(C.POINTER(C.c_float)))
     assert rc == 0
     return fine
+
+
+def ray_lib():
+    """liboracle's ray tracer (oracle/fd_ray.c)."""
+    lib = load_oracle()
+    if not getattr(lib, "_ray_bound", False):
+        from fdtomoc_gb300 import rayderv as R
+        lib.fdr_trace.argtypes = [C.POINTER(R.RayGrid), C.POINTER(C.POINTER(C.c_float)), C.c_int,
+                                  C.POINTER(R.RayObs), C.c_int, C.c_int, C.c_int, C.POINTER(R.RayResult),
+                                  C.POINTER(C.c_int), C.POINTER(C.c_float)]
+        lib.fdr_trace.restype = C.c_int
+        lib.fdr_trig.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double]
+        lib.fdr_trig.restype = C.c_double
+        lib._ray_bound = True
+    return lib
+
+
+def oracle_trace(trig_mode: int):
+    """A tracer for fdtomoc_gb300.rayderv.run: the oracle with the C library's trig functions
+    (trig_mode 0, as the reference) or the double-double ones the device uses (1)."""
+    import numpy as np
+    from fdtomoc_gb300 import rayderv as R
+
+    def trace(grid, fields, obs, nobs, cap):
+        lib = ray_lib()
+        n = max(1, nobs)
+        res = (R.RayResult * n)()
+        idx = np.zeros(n * cap, dtype=np.int32)
+        du = np.zeros(n * cap, dtype=np.float32)
+        fl = [np.ascontiguousarray(f, dtype=np.float32) for f in fields]
+        fp = (C.POINTER(C.c_float) * max(1, len(fl)))(*[f.ctypes.data_as(C.POINTER(C.c_float)) for f in fl])
+        rc = lib.fdr_trace(C.byref(grid), fp, nobs, obs, trig_mode, R.default_max_seg(grid), cap, res,
+                           idx.ctypes.data_as(C.POINTER(C.c_int)), du.ctypes.data_as(C.POINTER(C.c_float)))
+        assert rc == 0
+        return res, idx, du
+
+    return trace
