@@ -55,6 +55,8 @@ def parse():
     ap.add_argument("--locate-events", type=int, default=256,
                     help="events of the location leg (0: skip it)")
     ap.add_argument("--no-c2f", action="store_true", help="skip the c2f leg")
+    ap.add_argument("--ray-events", type=int, default=1024,
+                    help="events of the sphrayderv ray leg (0: skip it)")
     ap.add_argument("--profile-legs", action="store_true",
                     help="only run a small fixed case of the c2f and location kernels (for ncu captures)")
     args = ap.parse_args()
@@ -299,6 +301,96 @@ def locate_leg(args, lib, ctx, g, fields, stream):
                              "sample": f"{len(sample)} of the {E} events, the location oracle, one event per host thread"},
             "parity": {"events_checked": len(sample), "events_differing": mism, "bit_identical": mism == 0},
             "what": "sphfdloc grid search (node search, two refinements, outlier passes) per event"}
+
+
+def ray_leg(args, lib, ctx, g, sts, fields, stream):
+    """sphrayderv's rays (fdgpu_raytrace) through the batch step's 64 P fields still on the device:
+    args.ray_events synthetic events at random points inside the grid, each observed at 24-40 of the
+    stations, on a 21x21x17 coarse metagrid (every 10th node across, every 5th down).  Timed through
+    the public call (observations in from host memory, residuals, hypocentre derivatives and packed
+    coarse derivatives out).  CPU baseline: the ray oracle with the C library's trig functions (as
+    the reference's sphrayderv) on the host cores for a sample of the events; the same sample traced
+    with the oracle's double-double trig is compared with the GPU's results bit for bit."""
+    import ctypes as C
+    from concurrent.futures import ThreadPoolExecutor
+    import numpy as np
+    import torch
+    from fdtomoc_gb300 import rayderv as R
+    E = args.ray_events
+    sp = dict(nxc=21, nyc=21, nzc=17, igridx=[10] * 20, igridy=[10] * 20, igridz=[5] * 16, h=g.h, x0=g.x0, y0=g.y0,
+              z0=g.z0, dq=g.dlat, df=g.dlon)
+    assert 1 + sum(sp["igridx"]) == g.nx and 1 + sum(sp["igridy"]) == g.ny and 1 + sum(sp["igridz"]) == g.nz
+    grid, keep = R.grid_from_spec(sp)
+    st = [dict(xs=float(np.float32(s["lon"] * R.DEGRAD)), ys=float(np.float32(R.HPI - R.glat(s["lat"] * R.DEGRAD))),
+               zs=float(-np.float32(s["elev"]))) for s in sts[:len(fields)]]
+    rng = np.random.default_rng(11)
+    ns = len(fields)
+    obs = []
+    bounds = []
+    for e in range(E):
+        bounds.append(len(obs))
+        ex = grid.x0 + grid.df * rng.uniform(5, g.nx - 6)
+        ey = grid.y0 + grid.dq * rng.uniform(5, g.ny - 6)
+        ez = grid.z0 + grid.h * rng.uniform(6, g.nz - 6)
+        for k in rng.choice(ns, size=int(rng.integers(24, 41)), replace=False):
+            w = np.float32(rng.choice([0.05, 0.1, 0.2]))
+            obs.append(R.RayObs(ex, ey, ez, st[k]["xs"], st[k]["ys"], st[k]["zs"], int(k), 0,
+                                float(np.float32(rng.uniform(5, 40))), float(np.float32(1.0) / (w * w)),
+                                float(np.float32(0.0)), 0))
+    nobs = len(obs)
+    bounds = [(bounds[e], bounds[e + 1] if e + 1 < E else nobs) for e in range(E)]
+    arr = (R.RayObs * nobs)(*obs)
+    ptrs = [f.data_ptr() for f in fields]
+    cap = R.default_cap(grid)
+    lib.raytrace(ctx, grid, ptrs, arr, min(nobs, 256), cap=cap, stream_ptr=stream.cuda_stream)   # warm-up
+    torch.cuda.synchronize()
+    reps = 3
+    t0 = time.time()
+    for _ in range(reps):
+        got = lib.raytrace(ctx, grid, ptrs, arr, nobs, cap=cap, stream_ptr=stream.cuda_stream)
+    gpu_s = (time.time() - t0) / reps
+    res = got[0]
+    segs = sum(res[o].nseg for o in range(nobs))
+    ok = sum(1 for o in range(nobs) if res[o].status == R.RAY_OK)
+
+    # CPU: the oracle, a sample of events, one event's rays per host thread
+    build_oracle()
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from oracle_util import oracle_trace
+    host = [f.cpu().numpy().reshape(-1) for f in fields]
+    cores = os.cpu_count() or 1
+    sample = bounds[:min(E, 2 * cores)]
+
+    def one(b, mode):
+        a = (R.RayObs * (b[1] - b[0]))(*[arr[i] for i in range(b[0], b[1])])
+        return oracle_trace(mode)(grid, host, a, b[1] - b[0], cap)
+
+    t0 = time.time()
+    with ThreadPoolExecutor(cores) as ex:
+        list(ex.map(lambda b: one(b, 0), sample))
+    cpu_s = time.time() - t0
+    with ThreadPoolExecutor(cores) as ex:
+        exact = list(ex.map(lambda b: one(b, 1), sample))
+    mism = 0
+    for b, (rr, off, idx, du) in zip(sample, exact):
+        for i in range(b[1] - b[0]):
+            x, y = res[b[0] + i], rr[i]
+            a0, a1 = got[1][b[0] + i], got[1][b[0] + i + 1]
+            if (x.status, x.nseg, x.nnz, x.dt, bytes(x.am)) != (y.status, y.nseg, y.nnz, y.dt, bytes(y.am)) or \
+                    not np.array_equal(got[2][a0:a1], idx[off[i]:off[i + 1]]) or \
+                    got[3][a0:a1].tobytes() != du[off[i]:off[i + 1]].tobytes():
+                mism += 1
+    nsample = sum(b[1] - b[0] for b in sample)
+    del keep
+    return {"events": E, "rays": nobs, "fields": ns, "grid": [g.nx, g.ny, g.nz], "coarse": [21, 21, 17],
+            "rays_per_s": nobs / gpu_s, "wall_s": gpu_s, "reached_station": ok, "segments": segs,
+            "nonzero_derivatives": int(got[1][nobs]),
+            "cpu_baseline": {"rays_per_s": nsample / cpu_s, "cores": min(cores, len(sample)), "kind": "port",
+                             "sample": f"{len(sample)} of the {E} events ({nsample} rays), the ray oracle with the "
+                                       f"C library's trig, one event per host thread"},
+            "parity": {"rays_checked": nsample, "rays_differing": mism, "bit_identical": mism == 0},
+            "what": "sphrayderv per observation: residual, hypocentre derivatives, ray back-trace, coarse "
+                    "slowness derivatives"}
 
 
 def c2f_leg(args, lib, ctx, stream):
@@ -734,6 +826,7 @@ def run_gpu(args):
 
     locating = locate_leg(args, lib, ctx, g, fields, stream) if args.locate_events > 0 else None
     modelling = c2f_leg(args, lib, ctx, stream) if not args.no_c2f else None
+    tracing = ray_leg(args, lib, ctx, g, sts, fields, stream) if args.ray_events > 0 else None
     # the serving session's long-running grid waits on its host thread; under a profiler that
     # serialises launches the launching call would not return while the grid waits, so the leg is
     # left out there
@@ -788,6 +881,8 @@ def run_gpu(args):
             line["locate"] = locating
         if modelling is not None:
             line["c2f"] = modelling
+        if tracing is not None:
+            line["rays"] = tracing
         if cpu is not None:
             line["cpu_baseline"] = cpu
         print(json.dumps(line), flush=True)

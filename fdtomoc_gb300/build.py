@@ -51,7 +51,7 @@ def build(force: bool = False, verbose: bool = False, defines=(), lib_path: str 
     os.makedirs(os.path.dirname(EXE), exist_ok=True)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
     headers.append(os.path.join(ROOT, "include", "fdgpu.h"))
-    units = [("fdgpu_kernels.cu", []), ("fdgpu_host.cpp", []), ("fdgpu_noalloc.cu", []), ("fdgpu_serve.cpp", []), ("fdgpu_locate.cu", []), ("fdgpu_c2f.cu", [])]
+    units = [("fdgpu_kernels.cu", []), ("fdgpu_host.cpp", []), ("fdgpu_noalloc.cu", []), ("fdgpu_serve.cpp", []), ("fdgpu_locate.cu", []), ("fdgpu_c2f.cu", []), ("fdgpu_ray.cu", [])]
     objs = []
     jobs = []
     for src, extra in units:

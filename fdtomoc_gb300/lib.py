@@ -15,6 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.environ.get("FDGPU_LIB") or os.path.join(HERE, "libfdgpu.so")
 
 FDGPU_OK = 0
+FDGPU_ETOOBIG = -9
 ERRORS = {-1: "EINVAL", -2: "ENOMEM", -3: "ECUDA", -4: "EIO", -5: "EPAR", -6: "ESOURCE", -7: "ESCHED", -8: "ENODEV",
           -9: "ETOOBIG"}
 
@@ -149,6 +150,12 @@ def load() -> C.CDLL:
         lib.fdgpu_solve_device.argtypes = [P, C.c_int, C.POINTER(Station), C.c_void_p, C.c_longlong, C.c_longlong,
                                            C.POINTER(C.c_void_p), C.c_int, C.POINTER(Stats), C.c_void_p]
         lib.fdgpu_probe_fp64.argtypes = [P, C.POINTER(C.c_double)]
+        from . import rayderv as _R
+        lib.fdgpu_ray_default_limits.argtypes = [C.POINTER(_R.RayGrid), C.POINTER(C.c_int), C.POINTER(C.c_int)]
+        lib.fdgpu_raytrace.argtypes = [P, C.POINTER(_R.RayGrid), C.POINTER(C.c_void_p), C.c_int, C.c_int,
+                                       C.POINTER(_R.RayObs), C.c_int, C.c_int, C.POINTER(_R.RayResult),
+                                       C.POINTER(C.c_longlong), C.POINTER(C.c_int), C.POINTER(C.c_float),
+                                       C.c_longlong, C.c_void_p]
         lib.fdgpu_batch_create.argtypes = [P, C.c_int, C.POINTER(Station), C.c_void_p, C.c_longlong, C.c_longlong,
                                            C.POINTER(C.c_void_p), C.c_int, C.POINTER(P)]
         lib.fdgpu_batch_run.argtypes = [P, C.c_void_p]
@@ -277,6 +284,31 @@ class Context:
     def velocity_to_slowness(self, vel_ptr: int, slow_ptr: int, n: int, stream_ptr: int = 0):
         _check(self.lib.fdgpu_velocity_to_slowness(self.ptr, C.c_void_p(vel_ptr), C.c_void_p(slow_ptr), n,
                                                    C.c_void_p(stream_ptr)), self.ptr)
+
+
+def raytrace(ctx: "Context", grid, d_fields, obs, nobs: int, cap: int = 0, max_seg: int = 0, stream_ptr: int = 0,
+             total_cap: int | None = None):
+    """fdgpu_raytrace: returns (results, off, idx, du), observation o's derivatives at
+    idx/du[off[o] .. off[o+1])."""
+    from . import rayderv as R
+    lib = load()
+    n = max(1, nobs)
+    res = (R.RayResult * n)()
+    off = np.zeros(n + 1, dtype=np.int64)
+    fp = (C.c_void_p * max(1, len(d_fields)))(*d_fields)
+    if total_cap is None:
+        total_cap = 64 * max(1, nobs)
+    while True:
+        idx = np.zeros(max(1, total_cap), dtype=np.int32)
+        du = np.zeros(max(1, total_cap), dtype=np.float32)
+        rc = lib.fdgpu_raytrace(ctx.ptr, C.byref(grid), fp, len(d_fields), nobs, obs, max_seg, cap, res,
+                                off.ctypes.data_as(C.POINTER(C.c_longlong)), idx.ctypes.data_as(C.POINTER(C.c_int)),
+                                du.ctypes.data_as(C.POINTER(C.c_float)), total_cap, C.c_void_p(stream_ptr))
+        if rc == FDGPU_ETOOBIG and off[nobs] > total_cap:
+            total_cap = int(off[nobs])
+            continue
+        _check(rc, ctx.ptr)
+        return res, off[: nobs + 1], idx[: off[nobs]], du[: off[nobs]]
 
 
 class Batch:

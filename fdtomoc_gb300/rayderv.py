@@ -289,8 +289,9 @@ class Assembler:
         self.dth: list[str] = []
         self.bok: list[str] = []
 
-    def event(self, inside: bool, rows, results, idx, du, cap: int):
-        """One event: rows[i] = (observation index or -1, phase), results/idx/du the tracer's."""
+    def event(self, inside: bool, rows, results, off, idx, du):
+        """One event: rows[i] = (observation index or -1, phase); results, off, idx, du the tracer's
+        (observation o's derivatives at idx/du[off[o] .. off[o] + nnz))."""
         self.nev += 1
         if not inside:
             return
@@ -315,7 +316,7 @@ class Assembler:
             self.dat[i] = F32(r.dt * float(wet))
             am[i] = [F32(v) for v in r.am]
             nbk = 0
-            base = o * cap
+            base = int(off[o])
             for q in range(r.nnz):
                 jb = int(idx[base + q])
                 j = jb + (self.maxvarc if iph == 1 else 0)
@@ -380,8 +381,9 @@ def default_cap(grid: RayGrid) -> int:
 
 
 def run(specfile: str, trace, cap: int | None = None) -> dict[str, bytes]:
-    """sphrayderv on one spec: trace(grid, fields, obs, nobs, cap) -> (results, idx, du) does the
-    rays; returns the file contents by spec name (and writes them where the spec says)."""
+    """sphrayderv on one spec: trace(grid, fields, obs, nobs, cap) -> (results, off, idx, du) does
+    the rays (fields as host arrays); returns the file contents by spec name (and writes them where
+    the spec says)."""
     sp = read_spec(specfile)
     if sp["ivpvs"] or sp["dotel"] or sp["doshot"] or sp["nomat"]:
         raise ValueError("only local earthquakes with ivpvs 0 and nomat 0 are supported")
@@ -392,13 +394,31 @@ def run(specfile: str, trace, cap: int | None = None) -> dict[str, bytes]:
     tfields = load_fields(sp, grid, fields)
     if cap is None:
         cap = default_cap(grid)
-    results, idx, du = trace(grid, tfields, obs, nobs, cap)
+    results, off, idx, du = trace(grid, tfields, obs, nobs, cap)
     asm = Assembler(grid)
     for inside, rows in plan:
-        asm.event(inside, rows, results, idx, du, cap)
+        asm.event(inside, rows, results, off, idx, du)
     out = asm.files()
     for name, data in out.items():
         with open(sp[name], "wb") as fh:
             fh.write(data)
     del keep
     return out
+
+
+def gpu_trace(ctx=None, device: int = 0):
+    """A tracer for run(): the fields go to the device and fdgpu_raytrace traces the rays."""
+    from . import lib as L
+
+    def trace(grid, fields, obs, nobs, cap):
+        import torch
+        dev = [torch.from_numpy(np.ascontiguousarray(f, dtype=np.float32)).to(f"cuda:{device}") for f in fields]
+        own = ctx is None
+        c = L.Context(device) if own else ctx
+        try:
+            return L.raytrace(c, grid, [t.data_ptr() for t in dev], obs, nobs, cap=cap)
+        finally:
+            if own:
+                c.close()
+
+    return trace

@@ -341,6 +341,63 @@ int fdgpu_c2f_plan_create(fdgpu_ctx *ctx, const fdgpu_c2f_grid *g, fdgpu_c2f_pla
 int fdgpu_c2f_run(fdgpu_c2f_plan *plan, const float *d_coarse, float *d_fine, void *stream);
 void fdgpu_c2f_plan_destroy(fdgpu_c2f_plan *plan);
 
+/* ---- sphrayderv's rays on the device fields (reference src/sphrayderv.c:1054-2232) ----------
+ * For each observation (an event's phase at a station): the residual and hypocentre derivatives at
+ * the event (:1366-1441), the ray traced from the event back down the travel-time gradient to the
+ * station (:1444-2140), and its slowness derivatives on the coarse metagrid (:2155-2232), bit-
+ * identical to the oracle with correctly rounded sin/cos/atan2.  The event loop's bookkeeping and
+ * the output files stay with the caller (fdtomoc_gb300/rayderv.py writes them as the reference). */
+typedef struct fdgpu_ray_grid {
+    int nx, ny, nz;            /* fine grid */
+    int nxc, nyc, nzc;         /* coarse grid */
+    double x0, y0, z0;         /* origin: longitude (rad), geocentric colatitude (rad), depth (km) */
+    double h, dq, df;          /* km, rad, rad (:470-525) */
+    const float *gx, *gy, *gz; /* host: coarse node coordinates as the reference stores them (:779-788) */
+} fdgpu_ray_grid;
+
+typedef struct fdgpu_ray_obs {
+    double ex, ey, ez;         /* event: longitude, colatitude (rad), depth (km) (:924-927) */
+    double xs, ys, zs;         /* station: longitude, colatitude (rad), -elevation (km) (:835-838) */
+    int field;                 /* index into d_fields: the station-phase's time field */
+    int phase;                 /* 0 P, 1 S */
+    float obstime;             /* arrival minus origin (s) */
+    float pwt;                 /* 1 / rwt^2 */
+    float tc;                  /* station correction */
+    int pad;
+} fdgpu_ray_obs;
+
+enum {
+    FDGPU_RAY_OK = 0,          /* reached the station: derivatives valid */
+    FDGPU_RAY_NOTIME = 1,      /* a corner of the event's cell has no time (> 1e9) (:1357-1364) */
+    FDGPU_RAY_LEFT = 2,        /* the ray left the model (:2037-2140) */
+    FDGPU_RAY_STEPS = 3,       /* more than max_seg segments or cap derivatives (the reference has no limit) */
+    FDGPU_RAY_COARSE = 4,      /* a segment midpoint beyond the coarse grid (the reference asserts) */
+    FDGPU_RAY_OUTSIDE = 5,     /* a cell corner outside the field (the reference reads past it) */
+};
+
+typedef struct fdgpu_ray_result {
+    int status;
+    int nseg;
+    double dt;                 /* residual obstime - (t + tc) (:1397-1400) */
+    float resmin;              /* the same as float */
+    float wet;                 /* sqrt(pwt) */
+    float am[4];               /* wet, dt/dx wet, dt/dy wet, dt/dz wet (:1600-1604) */
+    int nnz;                   /* nonzero coarse derivatives */
+    int pad;
+} fdgpu_ray_result;
+
+/* Default limits for a grid: segments per ray and derivative entries per ray. */
+int fdgpu_ray_default_limits(const fdgpu_ray_grid *g, int *max_seg, int *cap);
+
+/* Trace nobs observations against device fields d_fields[0..nfields) (nz*ny*nx floats each).  obs and
+ * res are host arrays; observation k's nonzero derivatives (raw du before the sqrt(pwt) weight,
+ * ascending coarse node) go to idx/du[off[k] .. off[k+1]), off host (nobs+1), idx/du host arrays of
+ * total_cap entries (FDGPU_ETOOBIG if the run has more; off and res are filled either way).
+ * max_seg, cap <= 0: the defaults. */
+int fdgpu_raytrace(fdgpu_ctx *ctx, const fdgpu_ray_grid *g, const float *const *d_fields, int nfields, int nobs,
+                   const fdgpu_ray_obs *obs, int max_seg, int cap, fdgpu_ray_result *res, long long *off, int *idx,
+                   float *du, long long total_cap, void *stream);
+
 /* Drop-in sphfd(): ac/av as the reference's (av[1] = "par=<file>"), output_path = timedir.
  * Reads the velocity file, solves on the GPU, writes <output_path>/<timefile> byte-for-byte as
  * the reference does.  Uses a per-thread default context on device 0. */

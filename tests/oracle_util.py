@@ -181,6 +181,10 @@ def oracle_trace(trig_mode: int):
         rc = lib.fdr_trace(C.byref(grid), fp, nobs, obs, trig_mode, R.default_max_seg(grid), cap, res,
                            idx.ctypes.data_as(C.POINTER(C.c_int)), du.ctypes.data_as(C.POINTER(C.c_float)))
         assert rc == 0
-        return res, idx, du
+        nnz = np.array([res[o].nnz for o in range(nobs)], dtype=np.int64)
+        off = np.zeros(nobs + 1, dtype=np.int64)
+        np.cumsum(nnz, out=off[1:])
+        take = np.concatenate([o * cap + np.arange(nnz[o]) for o in range(nobs)]) if nobs else np.zeros(0, int)
+        return res, off, idx[take], du[take]
 
     return trace

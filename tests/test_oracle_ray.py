@@ -41,7 +41,7 @@ def test_cases_cover_the_failure_paths(tmp_path):
         g, keep = R.grid_from_spec(sp)
         obs, nobs, plan, fields = R.build_observations(sp, g, R.read_stations(sp["stafile"]),
                                                        R.read_events(sp["locdfil"]))
-        res, idx, du = oracle_trace(0)(g, R.load_fields(sp, g, fields), obs, nobs, R.default_cap(g))
+        res, off, idx, du = oracle_trace(0)(g, R.load_fields(sp, g, fields), obs, nobs, R.default_cap(g))
         seen |= {res[o].status for o in range(nobs)}
         first_fails += sum(1 for inside, rows in plan
                            if inside and rows and (rows[0][0] < 0 or res[rows[0][0]].status != R.RAY_OK))
