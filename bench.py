@@ -320,7 +320,7 @@ def ray_leg(args, lib, ctx, g, sts, fields, stream):
     sp = dict(nxc=21, nyc=21, nzc=17, igridx=[10] * 20, igridy=[10] * 20, igridz=[5] * 16, h=g.h, x0=g.x0, y0=g.y0,
               z0=g.z0, dq=g.dlat, df=g.dlon)
     assert 1 + sum(sp["igridx"]) == g.nx and 1 + sum(sp["igridy"]) == g.ny and 1 + sum(sp["igridz"]) == g.nz
-    grid, keep = R.grid_from_spec(sp)
+    grid, keep = R.grid_from_spec(sp, spacing_rule=False)   # the fields' own 0.005-degree spacing
     st = [dict(xs=float(np.float32(s["lon"] * R.DEGRAD)), ys=float(np.float32(R.HPI - R.glat(s["lat"] * R.DEGRAD))),
                zs=float(-np.float32(s["elev"]))) for s in sts[:len(fields)]]
     rng = np.random.default_rng(11)

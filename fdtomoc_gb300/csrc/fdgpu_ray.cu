@@ -111,7 +111,7 @@ struct RayList {
 
     __device__ __forceinline__ void add(int index, double v)
     {
-        for (int q = 0; q < n; q++)
+        for (int q = n - 1; q >= 0; q--)   /* the latest segments touch the latest nodes */
             if (li[q] == index) {
                 lv[q] = (float)((double)lv[q] + v);
                 return;
@@ -125,6 +125,65 @@ struct RayList {
         n++;
     }
 };
+
+/* sin and cos of the cell-wall angles a ray meets: rows y(j) = dq j + y0 and y(j) + dq, columns
+ * x(i) = df i + x0 and x(i) + df, for j in [0, ny], i in [0, nx]; the same double-double functions
+ * as everywhere else, so a table entry equals a direct call bit for bit */
+struct WallTrig {
+    const double4 *row;   /* (sin y, cos y, sin(y + dq), cos(y + dq)) */
+    const double4 *col;   /* (sin x, cos x, sin(x + df), cos(x + df)) */
+};
+
+__global__ void ray_wall_trig(RayGridDev g, double4 *row, double4 *col)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    fdt_dd s, c, s2, c2;
+    if (k <= g.ny) {
+        const double yj = g.dq * k + g.y0;
+        fdt_sincos_full(yj, &s, &c);
+        fdt_sincos_full(yj + g.dq, &s2, &c2);
+        row[k] = make_double4(s.hi + s.lo, c.hi + c.lo, s2.hi + s2.lo, c2.hi + c2.lo);
+    }
+    if (k <= g.nx) {
+        const double xi = g.df * k + g.x0;
+        fdt_sincos_full(xi, &s, &c);
+        fdt_sincos_full(xi + g.df, &s2, &c2);
+        col[k] = make_double4(s.hi + s.lo, c.hi + c.lo, s2.hi + s2.lo, c2.hi + c2.lo);
+    }
+}
+
+/* (sin, cos) of y(je) (second = 0) or y(je) + dq (second = 1); a direct call off the table */
+__device__ __forceinline__ void row_trig(const RayGridDev &g, const WallTrig &w, int je, int second, double *sn,
+                                         double *cs)
+{
+    if (je >= 0 && je <= g.ny) {
+        const double4 v = w.row[je];
+        *sn = second ? v.z : v.x;
+        *cs = second ? v.w : v.y;
+        return;
+    }
+    const double yj = g.dq * je + g.y0;
+    fdt_dd s, c;
+    fdt_sincos_full(second ? yj + g.dq : yj, &s, &c);
+    *sn = s.hi + s.lo;
+    *cs = c.hi + c.lo;
+}
+
+__device__ __forceinline__ void col_trig(const RayGridDev &g, const WallTrig &w, int ie, int second, double *sn,
+                                         double *cs)
+{
+    if (ie >= 0 && ie <= g.nx) {
+        const double4 v = w.col[ie];
+        *sn = second ? v.z : v.x;
+        *cs = second ? v.w : v.y;
+        return;
+    }
+    const double xi = g.df * ie + g.x0;
+    fdt_dd s, c;
+    fdt_sincos_full(second ? xi + g.df : xi, &s, &c);
+    *sn = s.hi + s.lo;
+    *cs = c.hi + c.lo;
+}
 
 /* one segment of length dlen with midpoint (xm, ym, zm) onto the coarse grid; false if the
  * midpoint is beyond it (where the reference asserts) */
@@ -173,7 +232,7 @@ __device__ bool add_segment(const RayGridDev &g, const float *gx, const float *g
     return true;
 }
 
-__global__ void __launch_bounds__(kRayBlock) ray_trace(RayGridDev g, const float *__restrict__ coarse,
+__global__ void __launch_bounds__(kRayBlock) ray_trace(RayGridDev g, WallTrig wt, const float *__restrict__ coarse,
                                                        const RayObsDev *__restrict__ obs, int nobs, int max_seg,
                                                        int cap, fdgpu_ray_result *__restrict__ res,
                                                        int *__restrict__ lidx, float *__restrict__ lval)
@@ -275,6 +334,20 @@ __global__ void __launch_bounds__(kRayBlock) ray_trace(RayGridDev g, const float
             r.am[3] = dtdz * wet;
         }
 
+        /* the station in the cartesian frame, for the last cells (src/sphrayderv.c:1812-1817) */
+        float x2, y2, z2;
+        {
+            const double rr = kRearth - zs;
+            fdt_dd sdd, cdd;
+            fdt_sincos_full(xs, &sdd, &cdd);
+            const double sxs = sdd.hi + sdd.lo, cxs = cdd.hi + cdd.lo;
+            fdt_sincos_full(ys, &sdd, &cdd);
+            const double sys_ = sdd.hi + sdd.lo, cys = cdd.hi + cdd.lo;
+            x2 = rr * sys_ * cxs;
+            y2 = rr * sys_ * sxs;
+            z2 = rr * cys;
+        }
+
         /* the ray (src/sphrayderv.c:1444-2232) */
         int iseg = 0, isegm1 = 0, isegm2 = 0;
         for (;;) {
@@ -284,7 +357,10 @@ __global__ void __launch_bounds__(kRayBlock) ray_trace(RayGridDev g, const float
             const float dxs = xx - xs, dys = yy - ys, dzs = zz - zs;
             const float rs = kRearth - zz;
             const float dqs = rs * dys;
-            const float dfs = rs * fdt_sin(yy) * dxs;
+            fdt_dd sdd, cdd;
+            fdt_sincos_full(yy, &sdd, &cdd);
+            double sinq = sdd.hi + sdd.lo, cosq = cdd.hi + cdd.lo;
+            const float dfs = rs * sinq * dxs;
             const float float_dlen = sqrtf(dfs * dfs + dqs * dqs + dzs * dzs);
             double dlen = float_dlen;
             if ((ie == iscell && je == jscell && ke == kscell) || (dlen < (h / 1000.f))) {
@@ -296,8 +372,10 @@ __global__ void __launch_bounds__(kRayBlock) ray_trace(RayGridDev g, const float
             if (!corners(g, ie, je, ke, ipt)) { r.status = FDGPU_RAY_OUTSIDE; break; }
             float tv[8];
             for (int q = 0; q < 8; q++) tv[q] = t[ipt[q]];
-            const double r1 = kRearth - zk, r2 = r1 - h, q1 = yj, q2 = q1 + dq;
-            const double sq1 = fdt_sin(q1), sq2 = fdt_sin(q2);
+            const double r1 = kRearth - zk, r2 = r1 - h;
+            double sq1, cq1, sq2, cq2;
+            row_trig(g, wt, je, 0, &sq1, &cq1);   /* q1 = yj */
+            row_trig(g, wt, je, 1, &sq2, &cq2);   /* q2 = yj + dq */
             double gradt[3];
             gradt[0] = ((tv[1] - tv[0]) / (r1 * sq1) + (tv[3] - tv[2]) / (r1 * sq2) + (tv[5] - tv[4]) / (r2 * sq1)
                         + (tv[7] - tv[6]) / (r2 * sq2)) / (4 * df);
@@ -306,23 +384,13 @@ __global__ void __launch_bounds__(kRayBlock) ray_trace(RayGridDev g, const float
             gradt[0] = gradt[0] * -1;
             gradt[1] = gradt[1] * -1;
 
-            fdt_dd sdd, cdd;
             fdt_sincos_full(xx, &sdd, &cdd);
             double sinf_ = sdd.hi + sdd.lo, cosf_ = cdd.hi + cdd.lo;
-            fdt_sincos_full(yy, &sdd, &cdd);
-            double sinq = sdd.hi + sdd.lo, cosq = cdd.hi + cdd.lo;
             double ro = kRearth - zz;
             const double xo = ro * sinq * cosf_, yo = ro * sinq * sinf_, zo = ro * cosq;
             double sx, sy, sz;
             if (ie >= (is - 2) && ie < (is + 2) && je >= (js - 2) && je < (js + 2) && ke >= (ks - 2)
                 && ke < (ks + 2)) {
-                const double rr = kRearth - zs;
-                fdt_sincos_full(xs, &sdd, &cdd);
-                const double sxs = sdd.hi + sdd.lo, cxs = cdd.hi + cdd.lo;
-                const double sys_ = fdt_sin(ys), cys = fdt_cos(ys);
-                const float x2 = rr * sys_ * cxs;
-                const float y2 = rr * sys_ * sxs;
-                const float z2 = rr * cys;
                 const double dx = x2 - xo, dy = y2 - yo, dz = z2 - zo;
                 const double dl = sqrt(dx * dx + dy * dy + dz * dz);
                 sx = dx / dl;
@@ -356,9 +424,13 @@ __global__ void __launch_bounds__(kRayBlock) ray_trace(RayGridDev g, const float
             }
             dd[1] = -1e20;
             if (gradt[1] != 0) {
-                fdt_sincos_full(gradt[1] < 0 ? yj : yj + dq, &sdd, &cdd);
-                sinq = sdd.hi + sdd.lo;
-                cosq = cdd.hi + cdd.lo;
+                if (gradt[1] < 0) {
+                    sinq = sq1;
+                    cosq = cq1;
+                } else {
+                    sinq = sq2;
+                    cosq = cq2;
+                }
                 if (fabs(cosq) > fabs(sinq)) {
                     const double tanq = sinq / cosq, tansq = tanq * tanq;
                     a = sx * sx + sy * sy - sz * sz * tansq;
@@ -379,9 +451,7 @@ __global__ void __launch_bounds__(kRayBlock) ray_trace(RayGridDev g, const float
             }
             dd[0] = -1e20;
             if (gradt[0] != 0) {
-                fdt_sincos_full(gradt[0] < 0 ? xi : xi + df, &sdd, &cdd);
-                sinf_ = sdd.hi + sdd.lo;
-                cosf_ = cdd.hi + cdd.lo;
+                col_trig(g, wt, ie, gradt[0] < 0 ? 0 : 1, &sinf_, &cosf_);
                 float d1;
                 if (fabs(cosf_) > fabs(sinf_)) {
                     const double tanf_ = sinf_ / cosf_;
@@ -583,7 +653,10 @@ extern "C" int fdgpu_raytrace(fdgpu_ctx *ctx, const fdgpu_ray_grid *g, const flo
     int *lidx, *didx;
     fdgpu_ray_result *dres;
     long long *doff;
+    double4 *drow, *dcol;
     RAY_CU(mem.get(&dobs, nobs));
+    RAY_CU(mem.get(&drow, (size_t)g->ny + 1));
+    RAY_CU(mem.get(&dcol, (size_t)g->nx + 1));
     RAY_CU(mem.get(&dcoarse, ncoarse));
     RAY_CU(mem.get(&dres, nobs));
     RAY_CU(mem.get(&lidx, (size_t)nobs * cap));
@@ -592,8 +665,11 @@ extern "C" int fdgpu_raytrace(fdgpu_ctx *ctx, const fdgpu_ray_grid *g, const flo
     RAY_CU(cudaMemcpyAsync(dobs, hobs.data(), sizeof(RayObsDev) * nobs, cudaMemcpyHostToDevice, st));
     RAY_CU(cudaMemcpyAsync(dcoarse, hc.data(), sizeof(float) * ncoarse, cudaMemcpyHostToDevice, st));
     const RayGridDev G{g->nx, g->ny, g->nz, g->nxc, g->nyc, g->nzc, g->x0, g->y0, g->z0, g->h, g->dq, g->df};
+    const int nwall = (g->nx > g->ny ? g->nx : g->ny) + 1;
+    ray_wall_trig<<<(nwall + 127) / 128, 128, 0, st>>>(G, drow, dcol);
+    RAY_CU(cudaGetLastError());
     ray_trace<<<(nobs + kRayBlock - 1) / kRayBlock, kRayBlock, sizeof(float) * ncoarse, st>>>(
-        G, dcoarse, dobs, nobs, max_seg, cap, dres, lidx, lval);
+        G, WallTrig{drow, dcol}, dcoarse, dobs, nobs, max_seg, cap, dres, lidx, lval);
     RAY_CU(cudaGetLastError());
     RAY_CU(cudaMemcpyAsync(res, dres, sizeof(fdgpu_ray_result) * nobs, cudaMemcpyDeviceToHost, st));
     RAY_CU(cudaStreamSynchronize(st));

@@ -114,8 +114,13 @@ def read_spec(path: str) -> dict:
     return sp
 
 
-def grid_from_spec(sp: dict):
-    """Fine and coarse grid (:470-525, :779-788).  Returns (RayGrid, arrays to keep alive)."""
+def grid_from_spec(sp: dict, spacing_rule: bool = True):
+    """Fine and coarse grid (:470-525, :779-788).  Returns (RayGrid, arrays to keep alive).
+
+    The reference replaces a spacing below 1e-4 rad (about 0.0057 degrees) by h / rearth (:515-518),
+    where sphfd keeps the spacing it is given: for finer grids the two programs' frames then differ
+    and rays aim at a station the field does not have.  spacing_rule=False keeps dq and df as given,
+    for tracing through fields computed with that spacing."""
     nx = 1 + sum(sp["igridx"])
     ny = 1 + sum(sp["igridy"])
     nz = 1 + sum(sp["igridz"])
@@ -124,9 +129,9 @@ def grid_from_spec(sp: dict):
     y0 = HPI - glat(sp["y0"] * DEGRAD)
     dq = sp["dq"] * DEGRAD
     df = sp["df"] * DEGRAD
-    if abs(dq) < 0.0001:
+    if abs(dq) < 0.0001 and (spacing_rule or dq == 0):
         dq = h / REARTH
-    if abs(df) < 0.0001:
+    if abs(df) < 0.0001 and (spacing_rule or df == 0):
         df = abs(h / (REARTH * math.sin(y0)))
     z0 = sp["z0"]
 
