@@ -14,7 +14,9 @@
  * A second kernel packs the lists into the caller's arrays. */
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <climits>
+#include <cmath>
 #include <cstring>
 #include <vector>
 
@@ -39,7 +41,7 @@ struct RayObsDev {
     double ex, ey, ez, xs, ys, zs;
     const float *t;
     float obstime, pwt, tc;
-    int pad;
+    int out;              /* the observation's index in the caller's arrays */
 };
 
 /* (int) of a double as x86-64 converts it: truncation, INT_MIN for NaN and out-of-range values */
@@ -102,27 +104,35 @@ __device__ __forceinline__ bool corners(const RayGridDev &g, int ie, int je, int
     return ok;
 }
 
-/* the ray's derivative list: li/lv hold n entries, at most cap */
+/* the ray's derivative list: li/lv hold n entries, at most cap.  A ray crosses several fine cells
+ * per coarse cell, and every segment in one coarse cell adds to the same eight nodes: their list
+ * positions are kept (pos, for coarse cell `cell`) so that those segments add without a search. */
 struct RayList {
     int *li;
     float *lv;
     int n, cap;
     bool over;
+    int cell;
+    int pos[8];
 
-    __device__ __forceinline__ void add(int index, double v)
+    /* list position of node `index` (appended if new); -1 when the list is full */
+    __device__ __forceinline__ int find(int index)
     {
         for (int q = n - 1; q >= 0; q--)   /* the latest segments touch the latest nodes */
-            if (li[q] == index) {
-                lv[q] = (float)((double)lv[q] + v);
-                return;
-            }
-        if (n >= cap) {
+            if (li[q] == index) return q;
+        if (n >= cap) return -1;
+        li[n] = index;
+        lv[n] = 0.0f;
+        return n++;
+    }
+
+    __device__ __forceinline__ void add_at(int q, double v)
+    {
+        if (q < 0) {
             over = true;
             return;
         }
-        li[n] = index;
-        lv[n] = (float)((double)0.0f + v);
-        n++;
+        lv[q] = (float)((double)lv[q] + v);
     }
 };
 
@@ -227,8 +237,13 @@ __device__ bool add_segment(const RayGridDev &g, const float *gx, const float *g
     jpt[5] = nk2 + nj + i1 + 1;
     jpt[6] = nk2 + nj2 + i1;
     jpt[7] = nk2 + nj2 + i1 + 1;
+    const int cell = (k1 * g.nyc + j1) * g.nxc + i1;
+    if (cell != L.cell) {
+        for (int q = 0; q < 8; q++) L.pos[q] = jpt[q] < nxyzc ? L.find(jpt[q]) : -2;
+        L.cell = cell;
+    }
     for (int q = 0; q < 8; q++)
-        if (jpt[q] < nxyzc) L.add(jpt[q], ds[q] * dlen);
+        if (L.pos[q] != -2) L.add_at(L.pos[q], ds[q] * dlen);
     return true;
 }
 
@@ -241,14 +256,21 @@ __global__ void __launch_bounds__(kRayBlock) ray_trace(RayGridDev g, WallTrig wt
     const int ncoarse = g.nxc + g.nyc + g.nzc;
     for (int q = threadIdx.x; q < ncoarse; q += blockDim.x) s_coarse[q] = coarse[q];
     __syncthreads();
-    const int o = blockIdx.x * blockDim.x + threadIdx.x;
-    if (o >= nobs) return;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nobs) return;
     const float *gx = s_coarse, *gy = s_coarse + g.nxc, *gz = s_coarse + g.nxc + g.nyc;
-    const RayObsDev ob = obs[o];
+    const RayObsDev ob = obs[k];
+    const int o = ob.out;
     const float *t = ob.t;
     fdgpu_ray_result r;
     memset(&r, 0, sizeof r);
-    RayList L{lidx + (size_t)o * cap, lval + (size_t)o * cap, 0, cap, false};
+    RayList L;
+    L.li = lidx + (size_t)o * cap;
+    L.lv = lval + (size_t)o * cap;
+    L.n = 0;
+    L.cap = cap;
+    L.over = false;
+    L.cell = -1;
 
     const double x0 = g.x0, y0 = g.y0, z0 = g.z0, h = g.h, dq = g.dq, df = g.df;
     const int nx = g.nx, ny = g.ny, nz = g.nz;
@@ -636,10 +658,21 @@ extern "C" int fdgpu_raytrace(fdgpu_ctx *ctx, const fdgpu_ray_grid *g, const flo
     if (cudaSetDevice(fdh_ctx_device(ctx)) != cudaSuccess) return FDGPU_ENODEV;
     cudaStream_t st = stream ? (cudaStream_t)stream : (cudaStream_t)fdh_ctx_stream(ctx);
 
-    std::vector<RayObsDev> hobs(nobs);
+    /* launch order: longest rays first (cells between event and station), so that a warp's rays end
+     * together; each result goes back to its observation's slot */
+    std::vector<int> order(nobs);
+    std::vector<double> span(nobs);
     for (int k = 0; k < nobs; k++) {
         const fdgpu_ray_obs &o = obs[k];
-        hobs[k] = RayObsDev{o.ex, o.ey, o.ez, o.xs, o.ys, o.zs, d_fields[o.field], o.obstime, o.pwt, o.tc, 0};
+        span[k] = std::fabs((o.ex - o.xs) / g->df) + std::fabs((o.ey - o.ys) / g->dq) + std::fabs((o.ez - o.zs) / g->h);
+        if (!(span[k] == span[k])) span[k] = 0;
+        order[k] = k;
+    }
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return span[a] > span[b]; });
+    std::vector<RayObsDev> hobs(nobs);
+    for (int q = 0; q < nobs; q++) {
+        const fdgpu_ray_obs &o = obs[order[q]];
+        hobs[q] = RayObsDev{o.ex, o.ey, o.ez, o.xs, o.ys, o.zs, d_fields[o.field], o.obstime, o.pwt, o.tc, order[q]};
     }
     const int ncoarse = g->nxc + g->nyc + g->nzc;
     std::vector<float> hc(ncoarse);

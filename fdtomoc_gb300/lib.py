@@ -297,7 +297,7 @@ def raytrace(ctx: "Context", grid, d_fields, obs, nobs: int, cap: int = 0, max_s
     off = np.zeros(n + 1, dtype=np.int64)
     fp = (C.c_void_p * max(1, len(d_fields)))(*d_fields)
     if total_cap is None:
-        total_cap = 64 * max(1, nobs)
+        total_cap = 192 * max(1, nobs)   # a long ray has a few hundred; a second run only beyond that
     while True:
         idx = np.zeros(max(1, total_cap), dtype=np.int32)
         du = np.zeros(max(1, total_cap), dtype=np.float32)
