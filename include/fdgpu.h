@@ -14,8 +14,10 @@
  *      fdgpu_station_from_par, fdgpu_solve_host, fdgpu_solve_device, fdgpu_solve_noalloc.
  *   3. A serving session (fdgpu_serve_*): models resident on the device, requests admitted as
  *      they arrive and solved by a long-running grid, with latency statistics.
- *   4. The path's neighbours on the device: fdgpu_c2f (c2f, the model's producer) and
- *      fdgpu_locate (sphfdloc's event location, a consumer of the fields).
+ *   4. The path's neighbours on the device: fdgpu_c2f (c2f, the model's producer), fdgpu_locate
+ *      (sphfdloc's event location) and fdgpu_raytrace (sphrayderv's rays and derivatives), with
+ *      fdgpu_sphrayderv, a drop-in for sphrayderv's main built on it.
+ *   Level 2 also has prepared batches (fdgpu_batch_*) whose launch can be captured in a CUDA graph.
  *
  * Conventions: every function returns an FDGPU_* status (0 = success) and never aborts; the
  * caller owns host buffers and any device buffers it passes in; the library owns its scratch,
@@ -397,6 +399,20 @@ int fdgpu_ray_default_limits(const fdgpu_ray_grid *g, int *max_seg, int *cap);
 int fdgpu_raytrace(fdgpu_ctx *ctx, const fdgpu_ray_grid *g, const float *const *d_fields, int nfields, int nobs,
                    const fdgpu_ray_obs *obs, int max_seg, int cap, fdgpu_ray_result *res, long long *off, int *idx,
                    float *du, long long total_cap, void *stream);
+
+/* The tracer a sphrayderv run calls: fdgpu_raytrace's contract with host fields (the default moves them
+ * to device 0 and calls fdgpu_raytrace). */
+typedef int (*fdgpu_ray_tracer)(void *user, const fdgpu_ray_grid *g, const float *const *h_fields, int nfields,
+                                int nobs, const fdgpu_ray_obs *obs, fdgpu_ray_result *res, long long *off, int *idx,
+                                float *du, long long total_cap);
+
+/* Drop-in sphrayderv (src/sphrayderv.c main) for local earthquakes: reads the spec file, its station
+ * list, event file and time files as the reference does, traces every observation (tracer NULL: on the
+ * GPU), and writes dtdsfil, resfile, dtdhfil, bookfil, sclefil and hitfile as the reference writes them.
+ * spacing_rule 1 replaces dq/df below 1e-4 rad by h/rearth as the reference does (:515-518); 0 keeps
+ * the spec's spacing (the spacing sphfd used for the fields).  Teleseisms, shots, ivpvs and nomat are
+ * refused with FDGPU_EINVAL. */
+int fdgpu_sphrayderv(const char *specfile, int spacing_rule, fdgpu_ray_tracer tracer, void *user);
 
 /* Drop-in sphfd(): ac/av as the reference's (av[1] = "par=<file>"), output_path = timedir.
  * Reads the velocity file, solves on the GPU, writes <output_path>/<timefile> byte-for-byte as

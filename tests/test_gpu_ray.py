@@ -85,3 +85,21 @@ def test_small_cap_reports_steps(gpu_lib, tmp_path):
         got = R.gpu_trace(ctx)(g, fields, obs, nobs, 4)
     _same_rays(got, want, nobs)
     assert any(got[0][o].status == R.RAY_STEPS for o in range(nobs))
+
+
+def test_cxx_drop_in_on_the_gpu(gpu_lib, tmp_path):
+    """fdgpu_sphrayderv with its default tracer (fields to the device, fdgpu_raytrace): the six files
+    equal the reference's."""
+    import ctypes as C
+    lib = gpu_lib.load()
+    lib.fdgpu_sphrayderv.argtypes = [C.c_char_p, C.c_int, C.c_void_p, C.c_void_p]
+    lib.fdgpu_sphrayderv.restype = C.c_int
+    for seed in (2, 3):
+        d = tmp_path / str(seed)
+        spec = RC.write_inputs(RC.make_case(seed), str(d))
+        assert lib.fdgpu_sphrayderv(spec.encode(), 1, None, None) == 0
+        sp = R.read_spec(spec)
+        gold = RC.load_golden(seed)
+        for name in RC.OUT_FILES:
+            with open(sp[name], "rb") as fh:
+                assert fh.read() == gold[name], f"seed {seed}: {name} differs"
