@@ -26,7 +26,7 @@ def main():
     exe = os.path.join(ROOT, "oracle", "_ref", "sphrayderv_ref")
     if not os.path.exists(exe):
         raise SystemExit("build the reference first: make -C oracle ref")
-    for seed in RC.SEEDS:
+    for seed in RC.SEEDS + RC.EXTRA_SEEDS:
         p = RC.make_case(seed)
         work = tempfile.mkdtemp(prefix=f"ray{seed}_")
         spec = RC.write_inputs(p, work)

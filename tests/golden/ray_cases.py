@@ -23,22 +23,31 @@ from fdtomoc_gb300.formats import VHead, write_grid
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 SEEDS = (1, 2, 3, 4, 5, 6)
+# further cases pinned on the CPU: 7 ivs 0 (S phases read the P tables), 8 dq = df = 0 (spacing from h),
+# 9 events inside their stations' cells, 10 a finer and larger grid
+EXTRA_SEEDS = (7, 8, 9, 10)
 
 
 def make_case(seed: int) -> dict:
     rng = np.random.default_rng(1000 + seed)
     nxc, nyc, nzc = int(rng.integers(5, 8)), int(rng.integers(5, 8)), int(rng.integers(4, 6))
+    big = seed == 10
     p = dict(seed=seed, nxc=nxc, nyc=nyc, nzc=nzc,
-             igridx=[int(v) for v in rng.integers(3, 8, nxc - 1)],
-             igridy=[int(v) for v in rng.integers(3, 8, nyc - 1)],
+             igridx=[int(v) for v in rng.integers(6 if big else 3, 12 if big else 8, nxc - 1)],
+             igridy=[int(v) for v in rng.integers(6 if big else 3, 12 if big else 8, nyc - 1)],
              igridz=[int(v) for v in rng.integers(2, 5, nzc - 1)],
-             h=float(rng.choice([1.0, 2.0])), x0=120.5, y0=23.5, z0=-1.0, dq=0.01, df=0.01,
+             h=0.5 if big else float(rng.choice([1.0, 2.0])), x0=120.5, y0=23.5, z0=-1.0,
+             dq=0.006 if big else 0.01, df=0.006 if big else 0.01,
              vp=6.0, vs=3.5, amp=float(rng.uniform(0.0, 0.05)), kx=float(rng.uniform(1, 3)),
-             ky=float(rng.uniform(1, 3)), ivs=1)
+             ky=float(rng.uniform(1, 3)), ivs=0 if seed == 7 else 1)
+    if seed == 8:
+        p["dq"] = p["df"] = 0.0
     nx, ny, nz = 1 + sum(p["igridx"]), 1 + sum(p["igridy"]), 1 + sum(p["igridz"])
     p.update(nx=nx, ny=ny, nz=nz)
-    lat_top, lat_bot = p["y0"], p["y0"] - (ny - 1) * p["dq"]
-    lon_w, lon_e = p["x0"], p["x0"] + (nx - 1) * p["df"]
+    dlat = p["dq"] or math.degrees(p["h"] / R.REARTH)
+    dlon = p["df"] or dlat / math.cos(math.radians(p["y0"]))
+    lat_top, lat_bot = p["y0"], p["y0"] - (ny - 1) * dlat
+    lon_w, lon_e = p["x0"], p["x0"] + (nx - 1) * dlon
     st = []
     for k in range(int(rng.integers(6, 10))):
         st.append(dict(name=f"ST{k:02d}", lat=round(float(rng.uniform(lat_bot + 0.02, lat_top - 0.02)), 5),
@@ -62,6 +71,10 @@ def make_case(seed: int) -> dict:
                   dep=round(float(rng.uniform(1.0, zmax - 1.5)), 3), picks=[])
         if e == 2 and seed % 3 == 0:
             ev["lon"] = round(lon_e + 0.05, 5)     # outside the model: the event is skipped
+        if seed == 9 and e % 2 == 0:               # in (or next to) a station's cell
+            s0 = st[e % len(st)]
+            ev["lat"], ev["lon"] = round(s0["lat"] + 0.0004, 5), round(s0["lon"] - 0.0004, 5)
+            ev["dep"] = round(float(rng.uniform(-0.5, 0.8)), 3)
         events.append(ev)
     p["events"] = events
     return p

@@ -19,7 +19,7 @@ from oracle_util import oracle_trace, ray_lib  # noqa: E402
 from fdtomoc_gb300 import rayderv as R  # noqa: E402
 
 
-@pytest.mark.parametrize("seed", RC.SEEDS)
+@pytest.mark.parametrize("seed", RC.SEEDS + RC.EXTRA_SEEDS)
 @pytest.mark.parametrize("trig", [0, 1])
 def test_files_equal_reference(seed, trig, tmp_path):
     p = RC.make_case(seed)
@@ -34,7 +34,7 @@ def test_cases_cover_the_failure_paths(tmp_path):
     """rays that leave the model, cells without times, events whose first phase fails"""
     seen = set()
     first_fails = 0
-    for seed in RC.SEEDS:
+    for seed in RC.SEEDS + RC.EXTRA_SEEDS:
         p = RC.make_case(seed)
         spec = RC.write_inputs(p, str(tmp_path / str(seed)))
         sp = R.read_spec(spec)

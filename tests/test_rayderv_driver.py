@@ -57,7 +57,7 @@ def _bind():
     return lib
 
 
-@pytest.mark.parametrize("seed", RC.SEEDS)
+@pytest.mark.parametrize("seed", RC.SEEDS + RC.EXTRA_SEEDS)
 @pytest.mark.parametrize("trig", [0, 1])
 def test_drop_in_files_equal_reference(seed, trig, tmp_path):
     lib = _bind()
