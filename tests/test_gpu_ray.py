@@ -44,7 +44,7 @@ def _same_rays(a, b, nobs):
     assert np.array_equal(da.view(np.int32), db.view(np.int32))
 
 
-@pytest.mark.parametrize("seed", RC.SEEDS)
+@pytest.mark.parametrize("seed", RC.SEEDS + RC.EXTRA_SEEDS)
 def test_rays_equal_oracle_and_files_equal_reference(gpu_lib, seed, tmp_path):
     spec, sp, g, keep, obs, nobs, plan, fields = _setup(seed, str(tmp_path))
     cap = R.default_cap(g)
