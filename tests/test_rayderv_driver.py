@@ -88,3 +88,15 @@ def test_drop_in_missing_spec_entry(tmp_path):
     p = tmp_path / "spec"
     p.write_text("nxc 5\nnyc 5\n")
     assert lib.fdgpu_sphrayderv(str(p).encode(), 1, _oracle_tracer(0, []), None) == -5
+
+
+def test_default_tracer_without_a_device_is_an_error(tmp_path):
+    """no CPU fallback: with no GPU, the drop-in's default tracer reports it"""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    lib = L.load()
+    lib.fdgpu_sphrayderv.argtypes = [C.c_char_p, C.c_int, C.c_void_p, C.c_void_p]
+    spec = RC.write_inputs(RC.make_case(1), str(tmp_path))
+    rc = lib.fdgpu_sphrayderv(spec.encode(), 1, None, None)
+    assert rc in (-8, -3), rc
