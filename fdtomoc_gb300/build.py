@@ -1,4 +1,5 @@
-"""Build of libfdgpu.so and the drop-in sphfd and sphrayderv executables for sm_103a (nvcc, no cmake)."""
+"""Build of libfdgpu.so and the drop-in sphfd, sphfdloc and sphrayderv executables for sm_103a (nvcc, no
+cmake)."""
 from __future__ import annotations
 
 import concurrent.futures as cf
@@ -13,6 +14,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libfdgpu.so")
 EXE = os.path.join(HERE, "bin", "sphfd_gpu")
 EXE_RAY = os.path.join(HERE, "bin", "sphrayderv_gpu")
+EXE_LOC = os.path.join(HERE, "bin", "sphfdloc_gpu")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # --fmad=false: the solver's FP64 arithmetic must not be contracted into fused multiply-adds;
@@ -52,7 +54,7 @@ def build(force: bool = False, verbose: bool = False, defines=(), lib_path: str 
     os.makedirs(os.path.dirname(EXE), exist_ok=True)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
     headers.append(os.path.join(ROOT, "include", "fdgpu.h"))
-    units = [("fdgpu_kernels.cu", []), ("fdgpu_host.cpp", []), ("fdgpu_noalloc.cu", []), ("fdgpu_serve.cpp", []), ("fdgpu_locate.cu", []), ("fdgpu_c2f.cu", []), ("fdgpu_ray.cu", []), ("fdgpu_rayderv.cpp", [])]
+    units = [("fdgpu_kernels.cu", []), ("fdgpu_host.cpp", []), ("fdgpu_noalloc.cu", []), ("fdgpu_serve.cpp", []), ("fdgpu_locate.cu", []), ("fdgpu_c2f.cu", []), ("fdgpu_ray.cu", []), ("fdgpu_rayderv.cpp", []), ("fdgpu_sphfdloc.cpp", [])]
     objs = []
     jobs = []
     for src, extra in units:
@@ -69,7 +71,7 @@ def build(force: bool = False, verbose: bool = False, defines=(), lib_path: str 
         _run([nvcc] + ARCH + ["-shared", "-cudart", "static", "-o", lib_out] + objs + ["-lpthread"])
     if lib_path:
         return lib_out
-    for exe, main in ((EXE, "sphfd_main.cpp"), (EXE_RAY, "sphrayderv_main.cpp")):
+    for exe, main in ((EXE, "sphfd_main.cpp"), (EXE_RAY, "sphrayderv_main.cpp"), (EXE_LOC, "sphfdloc_main.cpp")):
         main = os.path.join(CSRC, main)
         if force or _stale(exe, [main, LIB]):
             _run([nvcc] + ARCH + NVFLAGS + [main, "-o", exe, "-L" + HERE, "-lfdgpu", "-Xlinker", "-rpath=" + HERE])

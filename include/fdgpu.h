@@ -16,7 +16,7 @@
  *      they arrive and solved by a long-running grid, with latency statistics.
  *   4. The path's neighbours on the device: fdgpu_c2f (c2f, the model's producer), fdgpu_locate
  *      (sphfdloc's event location) and fdgpu_raytrace (sphrayderv's rays and derivatives), with
- *      fdgpu_sphrayderv, a drop-in for sphrayderv's main built on it.
+ *      fdgpu_sphfdloc and fdgpu_sphrayderv, drop-ins for those programs' main built on them.
  *   Level 2 also has prepared batches (fdgpu_batch_*) whose launch can be captured in a CUDA graph.
  *
  * Conventions: every function returns an FDGPU_* status (0 = success) and never aborts; the
@@ -399,6 +399,18 @@ int fdgpu_ray_default_limits(const fdgpu_ray_grid *g, int *max_seg, int *cap);
 int fdgpu_raytrace(fdgpu_ctx *ctx, const fdgpu_ray_grid *g, const float *const *d_fields, int nfields, int nobs,
                    const fdgpu_ray_obs *obs, int max_seg, int cap, fdgpu_ray_result *res, long long *off, int *idx,
                    float *du, long long total_cap, void *stream);
+
+/* The locator a sphfdloc run calls: fdgpu_locate's contract with host fields (the default moves them to
+ * device 0 and calls fdgpu_locate). */
+typedef int (*fdgpu_loc_locator)(void *user, const fdgpu_loc_grid *g, const float *const *h_fields, int nfields,
+                                 int nev, const int *obs_offset, fdgpu_loc_obs *obs, float *resmin, float *tps,
+                                 fdgpu_loc_result *results);
+
+/* Drop-in sphfdloc (src/sphfdloc.c main): reads the spec, its event file (leqsfil) and the time files its
+ * phases name (<timedir>/<station>.ptimes|.stimes), locates every event (locator NULL: on the GPU), and
+ * writes fhedfil, fdatfil, fsumfil and outlfil as the reference writes them.  The per-event split under
+ * eqkdir and the log file are not made. */
+int fdgpu_sphfdloc(const char *specfile, fdgpu_loc_locator locator, void *user);
 
 /* The tracer a sphrayderv run calls: fdgpu_raytrace's contract with host fields (the default moves them
  * to device 0 and calls fdgpu_raytrace). */
