@@ -114,6 +114,7 @@ def test_gpu_locations_random_cases(gpu_lib, seed, shape, ivs):
         assert same(got[e], want) is None, (e, same(got[e], want))
 
 
+@pytest.mark.gpu
 def test_cxx_sphfdloc_drop_in_on_the_gpu(gpu_lib, tmp_path):
     """fdgpu_sphfdloc with its default locator (fields to the device, fdgpu_locate): the four reports
     equal the reference sphfdloc's"""
