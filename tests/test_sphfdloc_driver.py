@@ -79,3 +79,17 @@ def test_drop_in_missing_time_file(tmp_path):
     spec = LC.write_reference_inputs(p, str(tmp_path))
     os.remove(os.path.join(str(tmp_path), "ttimes", p["stations"][0]["name"] + ".ptimes"))
     assert lib.fdgpu_sphfdloc(spec.encode(), _oracle_locator([]), None) == -4
+
+
+def test_drop_in_refuses_a_marked_input_phase(tmp_path):
+    """an input phase marked '*' leaves the reference's parser a blank phase code, and it aborts
+    (src/sphfdloc.c:643-650); the drop-in returns FDGPU_EPAR"""
+    lib = _bind()
+    p, _ = LC.load_golden(1)
+    spec = LC.write_reference_inputs(p, str(tmp_path))
+    ev = os.path.join(str(tmp_path), "events.txt")
+    lines = open(ev).read().split("\n")
+    lines[1] = lines[1].replace(" P ", "*P ").replace(" S ", "*S ")
+    with open(ev, "w") as fh:
+        fh.write("\n".join(lines))
+    assert lib.fdgpu_sphfdloc(spec.encode(), _oracle_locator([]), None) == -5
