@@ -113,19 +113,3 @@ def test_gpu_locations_random_cases(gpu_lib, seed, shape, ivs):
         want = oracle_locate(grid_o, host, ob)
         assert same(got[e], want) is None, (e, same(got[e], want))
 
-
-@pytest.mark.gpu
-def test_cxx_sphfdloc_drop_in_on_the_gpu(gpu_lib, tmp_path):
-    """fdgpu_sphfdloc with its default locator (fields to the device, fdgpu_locate): the four reports
-    equal the reference sphfdloc's"""
-    import ctypes as C
-    lib = gpu_lib.load()
-    lib.fdgpu_sphfdloc.argtypes = [C.c_char_p, C.c_void_p, C.c_void_p]
-    lib.fdgpu_sphfdloc.restype = C.c_int
-    for seed in (1, 5):
-        p, gold = LC.load_golden(seed)
-        d = tmp_path / str(seed)
-        spec = LC.write_reference_inputs(p, str(d))
-        assert lib.fdgpu_sphfdloc(spec.encode(), None, None) == 0
-        for k, name in (("fhd", "fhd.txt"), ("dat", "dat.txt"), ("sum", "sum.txt"), ("out", "out.txt")):
-            assert (d / "out" / name).read_text() == gold[k], f"seed {seed}: {name} differs"
