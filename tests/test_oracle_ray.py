@@ -70,3 +70,23 @@ def test_double_double_trig_is_within_one_ulp_of_libm():
             diff += 1
             assert abs(a - b) <= math.ulp(b)
     assert diff <= n * 0.01
+
+
+def test_double_double_trig_is_correctly_rounded():
+    """sin, cos and atan2 of fd_trig.h against 40-digit values: every result is the correctly rounded
+    double (the functions the device uses; see the module for the method)"""
+    mp = pytest.importorskip("mpmath")
+    mp.mp.dps = 40
+    lib = ray_lib()
+    rng = np.random.default_rng(23)
+    bad = []
+    for x in np.concatenate([rng.uniform(-7.0, 7.0, 1500), rng.uniform(0.3, 2.3, 1500)]):
+        if lib.fdr_trig(1, 0, x, 0.0) != float(mp.sin(mp.mpf(x))):
+            bad.append(("sin", x))
+        if lib.fdr_trig(1, 1, x, 0.0) != float(mp.cos(mp.mpf(x))):
+            bad.append(("cos", x))
+    for _ in range(1500):
+        y, x = rng.uniform(-7000, 7000), rng.uniform(-7000, 7000)
+        if lib.fdr_trig(1, 2, y, x) != float(mp.atan2(mp.mpf(y), mp.mpf(x))):
+            bad.append(("atan2", y, x))
+    assert not bad, bad[:5]
