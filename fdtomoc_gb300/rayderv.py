@@ -427,3 +427,33 @@ def gpu_trace(ctx=None, device: int = 0):
                 c.close()
 
     return trace
+
+
+def sharded(trace, group=None):
+    """A tracer that splits the observations over the ranks of a torch.distributed group: rank r traces
+    the r-th contiguous slice with `trace` (on its own GPU), and one all-gather of the results gives
+    every rank the whole run, in observation order, so that each can write the files.  Observations are
+    independent; the tracing itself exchanges nothing."""
+
+    def run(grid, fields, obs, nobs, cap):
+        import torch.distributed as dist
+        world = dist.get_world_size(group)
+        rank = dist.get_rank(group)
+        lo, hi = nobs * rank // world, nobs * (rank + 1) // world
+        sub = (RayObs * max(1, hi - lo))(*[obs[i] for i in range(lo, hi)])
+        res, off, idx, du = trace(grid, fields, sub, hi - lo, cap)
+        mine = (C.string_at(C.addressof(res), C.sizeof(RayResult) * (hi - lo)),
+                np.asarray(idx[: int(off[hi - lo])], dtype=np.int32).tobytes(),
+                np.asarray(du[: int(off[hi - lo])], dtype=np.float32).tobytes())
+        parts = [None] * world
+        dist.all_gather_object(parts, mine, group=group)
+        all_res = (RayResult * max(1, nobs))()
+        raw = b"".join(p[0] for p in parts)
+        C.memmove(C.addressof(all_res), raw, len(raw))
+        idx_all = np.frombuffer(b"".join(p[1] for p in parts), dtype=np.int32)
+        du_all = np.frombuffer(b"".join(p[2] for p in parts), dtype=np.float32)
+        off_all = np.zeros(nobs + 1, dtype=np.int64)
+        np.cumsum([all_res[o].nnz for o in range(nobs)], out=off_all[1:])
+        return all_res, off_all, idx_all, du_all
+
+    return run
