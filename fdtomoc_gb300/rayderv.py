@@ -385,14 +385,14 @@ def default_cap(grid: RayGrid) -> int:
     return 8 * (grid.nx + grid.ny + grid.nz) + 64
 
 
-def run(specfile: str, trace, cap: int | None = None) -> dict[str, bytes]:
+def run(specfile: str, trace, cap: int | None = None, spacing_rule: bool = True) -> dict[str, bytes]:
     """sphrayderv on one spec: trace(grid, fields, obs, nobs, cap) -> (results, off, idx, du) does
     the rays (fields as host arrays); returns the file contents by spec name (and writes them where
-    the spec says)."""
+    the spec says).  spacing_rule: as grid_from_spec."""
     sp = read_spec(specfile)
     if sp["ivpvs"] or sp["dotel"] or sp["doshot"] or sp["nomat"]:
         raise ValueError("only local earthquakes with ivpvs 0 and nomat 0 are supported")
-    grid, keep = grid_from_spec(sp)
+    grid, keep = grid_from_spec(sp, spacing_rule)
     stations = read_stations(sp["stafile"])
     events = read_events(sp["locdfil"])
     obs, nobs, plan, fields = build_observations(sp, grid, stations, events)
