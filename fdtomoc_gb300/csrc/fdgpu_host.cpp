@@ -88,6 +88,7 @@ uint64_t bits(double x)
 struct fdgpu_ctx {
     int device = 0;
     int cluster = 0;   /* CTAs per station: 0 automatic */
+    long long wait_cycles = 0, walk_cycles = 0;   /* bounds of the solver's waits, 0: built-in */
     cudaStream_t stream = nullptr;
     std::map<GeoKey, std::unique_ptr<Geo>> geos;
     BatchBufs batch;   /* the buffers of fdgpu_solve_device, kept for the next call */
@@ -249,6 +250,14 @@ extern "C" int fdgpu_set_cluster(fdgpu_ctx *ctx, int ctas_per_station)
     return FDGPU_OK;
 }
 
+extern "C" int fdgpu_set_wait_limits(fdgpu_ctx *ctx, long long wait_cycles, long long walk_cycles)
+{
+    if (!ctx || wait_cycles < 0 || walk_cycles < 0) return FDGPU_EINVAL;
+    ctx->wait_cycles = wait_cycles;
+    ctx->walk_cycles = walk_cycles;
+    return FDGPU_OK;
+}
+
 namespace {
 
 /* Check the stations and lay out their records in bufs (queued on cs): everything a launch of
@@ -287,6 +296,8 @@ int prepare_batch(fdgpu_ctx *ctx, int n, const fdgpu_station *st, const float *s
         fdh::fill_station(hs[k], s, gp, d_times[k], slowness, s_sy, s_sz,
                           (s.srctype == 1 && !times_initialised) ? 0 : 1, base, base + fdh::face_bytes(s),
                           bufs.trig.as<double>() + (size_t)maxt * k, bufs.stats.as<fd_station_stats>() + k);
+        hs[k].wait_cycles = ctx->wait_cycles;
+        hs[k].walk_cycles = ctx->walk_cycles;
         max_pad = std::max(max_pad, hs[k].max_face_pad);
     }
     /* Launch order: largest grids first.  CTA i solves record i, and CTAs beyond the resident ones
@@ -387,6 +398,79 @@ extern "C" int fdgpu_batch_stats(fdgpu_batch *b, fdgpu_stats *stats, void *strea
     if (!b) return FDGPU_EINVAL;
     fdgpu_ctx *ctx = b->ctx;
     return read_stats(ctx, b->bufs.stats, b->n, stats, stream ? (cudaStream_t)stream : ctx->stream);
+}
+
+namespace {
+
+/* the batch's records as they sit on the device, in launch order, with the caller's index of each
+ * (its statistics slot) */
+int batch_records(fdgpu_batch *b, std::vector<fd_station_dev> &rec, std::vector<int> &idx, cudaStream_t cs)
+{
+    fdgpu_ctx *ctx = b->ctx;
+    rec.resize(b->n);
+    idx.resize(b->n);
+    FD_CU(ctx, cudaMemcpyAsync(rec.data(), b->bufs.stations.p, sizeof(fd_station_dev) * b->n, cudaMemcpyDeviceToHost, cs));
+    FD_CU(ctx, cudaStreamSynchronize(cs));
+    const fd_station_stats *base = b->bufs.stats.as<fd_station_stats>();
+    for (int k = 0; k < b->n; k++) idx[k] = (int)(rec[k].stats - base);
+    return FDGPU_OK;
+}
+
+}  // namespace
+
+extern "C" int fdgpu_batch_order(fdgpu_batch *b, int *order, void *stream)
+{
+    if (!b || !order) return FDGPU_EINVAL;
+    std::vector<fd_station_dev> rec;
+    std::vector<int> idx;
+    const int rc = batch_records(b, rec, idx, stream ? (cudaStream_t)stream : b->ctx->stream);
+    if (rc) return rc;
+    for (int k = 0; k < b->n; k++) order[k] = idx[k];
+    return FDGPU_OK;
+}
+
+extern "C" int fdgpu_batch_set_order(fdgpu_batch *b, const int *order, void *stream)
+{
+    if (!b || !order) return FDGPU_EINVAL;
+    fdgpu_ctx *ctx = b->ctx;
+    cudaStream_t cs = stream ? (cudaStream_t)stream : ctx->stream;
+    std::vector<char> seen(b->n, 0);
+    for (int k = 0; k < b->n; k++) {
+        if (order[k] < 0 || order[k] >= b->n || seen[order[k]]) return FDGPU_EINVAL;
+        seen[order[k]] = 1;
+    }
+    std::vector<fd_station_dev> rec, out(b->n);
+    std::vector<int> idx;
+    int rc = batch_records(b, rec, idx, cs);
+    if (rc) return rc;
+    std::vector<int> at(b->n);
+    for (int k = 0; k < b->n; k++) at[idx[k]] = k;
+    for (int k = 0; k < b->n; k++) out[k] = rec[at[order[k]]];
+    FD_CU(ctx, cudaMemcpyAsync(b->bufs.stations.p, out.data(), sizeof(fd_station_dev) * b->n, cudaMemcpyHostToDevice, cs));
+    FD_CU(ctx, cudaStreamSynchronize(cs));
+    return FDGPU_OK;
+}
+
+extern "C" int fdgpu_batch_tune_order(fdgpu_batch *b, void *stream)
+{
+    if (!b) return FDGPU_EINVAL;
+    fdgpu_ctx *ctx = b->ctx;
+    cudaStream_t cs = stream ? (cudaStream_t)stream : ctx->stream;
+    std::vector<fd_station_dev> rec;
+    std::vector<int> idx;
+    int rc = batch_records(b, rec, idx, cs);
+    if (rc) return rc;
+    std::vector<fd_station_stats> hst(b->n);
+    FD_CU(ctx, cudaMemcpyAsync(hst.data(), b->bufs.stats.p, sizeof(fd_station_stats) * b->n, cudaMemcpyDeviceToHost, cs));
+    FD_CU(ctx, cudaStreamSynchronize(cs));
+    for (int k = 0; k < b->n; k++)
+        if (hst[k].t_end_ns <= hst[k].t_start_ns || hst[k].status) return FDGPU_EINVAL;   /* no clean run yet */
+    /* longest measured solve first; equal times keep the current order */
+    std::vector<int> order(idx);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int c) {
+        return hst[a].t_end_ns - hst[a].t_start_ns > hst[c].t_end_ns - hst[c].t_start_ns;
+    });
+    return fdgpu_batch_set_order(b, order.data(), stream);
 }
 
 extern "C" void fdgpu_batch_destroy(fdgpu_batch *b)
@@ -784,8 +868,10 @@ fdgpu_ctx *default_ctx(int *status)
     return ctx;
 }
 
-/* solve a set of parsed par files and write their time files */
-void run_setups(fdgpu_ctx *ctx, std::vector<ParSetup> &ps, std::vector<int> &stat, const char *output_path)
+/* solve a set of parsed par files and write their time files.  Every input (par file, velocity
+ * file, starting field) is read and checked before the GPU is touched: the context is created on
+ * the first solve, so a run whose inputs are all bad returns their statuses without a device. */
+void run_setups(std::vector<ParSetup> &ps, std::vector<int> &stat, const char *output_path)
 {
     const int n = (int)ps.size();
     /* group stations by velocity file and grid so each model is read and uploaded once */
@@ -824,8 +910,10 @@ void run_setups(fdgpu_ctx *ctx, std::vector<ParSetup> &ps, std::vector<int> &sta
             if (bad) { for (int k : sel) if (!stat[k]) stat[k] = FDGPU_EIO; continue; }
             std::vector<fdgpu_stats> sst(sel.size());
             const fdgpu_station &s0 = sts[0];
-            rc = fdgpu_solve_host(ctx, (int)sts.size(), sts.data(), vel.data(), s0.nx, s0.ny, s0.nz, outp.data(),
-                                  pass == 1 ? initp.data() : nullptr, sst.data());
+            fdgpu_ctx *ctx = default_ctx(&rc);
+            if (ctx)
+                rc = fdgpu_solve_host(ctx, (int)sts.size(), sts.data(), vel.data(), s0.nx, s0.ny, s0.nz, outp.data(),
+                                      pass == 1 ? initp.data() : nullptr, sst.data());
             for (size_t j = 0; j < sel.size(); j++) {
                 if (rc) { stat[sel[j]] = rc; continue; }
                 stat[sel[j]] = write_times(ps[sel[j]], hin, out[j], output_path);
@@ -852,16 +940,13 @@ extern "C" int fdgpu_station_from_par(int ac, char **av, fdgpu_station *st, char
 extern "C" int fdgpu_sphfd_parlist(int n, char **entries, const char *output_path, int *status)
 {
     if (n < 0 || (n > 0 && !entries) || !output_path) return FDGPU_EINVAL;
-    int rc0 = FDGPU_OK;
-    fdgpu_ctx *ctx = default_ctx(&rc0);
-    if (!ctx) return rc0;
     std::vector<ParSetup> ps(n);
     std::vector<int> stat(n, FDGPU_OK);
     for (int k = 0; k < n; k++) {
         char *av[2] = {(char *)"sphfd", entries[k]};
         stat[k] = setup_from_par(2, av, ps[k]);
     }
-    run_setups(ctx, ps, stat, output_path);
+    run_setups(ps, stat, output_path);
     int first = FDGPU_OK;
     for (int k = 0; k < n; k++) {
         if (status) status[k] = stat[k];
@@ -873,11 +958,8 @@ extern "C" int fdgpu_sphfd_parlist(int n, char **entries, const char *output_pat
 extern "C" int fdgpu_sphfd(int ac, char **av, const char *output_path)
 {
     if (ac < 1 || !av || !output_path) return FDGPU_EINVAL;
-    int rc0 = FDGPU_OK;
-    fdgpu_ctx *ctx = default_ctx(&rc0);
-    if (!ctx) return rc0;
     std::vector<ParSetup> ps(1);
     std::vector<int> stat(1, setup_from_par(ac, av, ps[0]));
-    run_setups(ctx, ps, stat, output_path);
+    run_setups(ps, stat, output_path);
     return stat[0];
 }

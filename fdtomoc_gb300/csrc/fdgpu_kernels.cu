@@ -1384,6 +1384,8 @@ __device__ void run_walk(const fd_station_dev &sd, Shared &sh, const CtaSmem &cs
     bool idle = false;
     long long since = clock64();
     const long long started = since;
+    const long long wait_lim = sd.wait_cycles > 0 ? sd.wait_cycles : FD_WAIT_CYCLES;
+    const long long walk_lim = sd.walk_cycles > 0 ? sd.walk_cycles : FD_WALK_CYCLES;
     long long chunks = 0;
     for (;;) {
         int act = 0, h = 0, m = 0, qf = 0;   /* act: 0 wait, 1 chunk, 2 resume a waiter, 3 leave */
@@ -1421,11 +1423,11 @@ __device__ void run_walk(const fd_station_dev &sd, Shared &sh, const CtaSmem &cs
                 }
                 if (act == 1 || act == 2) {
                     since = clock64();
-                } else if (act == 0 && clock64() - since > FD_WAIT_CYCLES) {
+                } else if (act == 0 && clock64() - since > wait_lim) {
                     atomicCAS(&sh.w->status, 0, 8);   /* no work for this worker for too long */
                     act = 3;
                 }
-                if (act != 3 && clock64() - started > FD_WALK_CYCLES) {
+                if (act != 3 && clock64() - started > walk_lim) {
                     atomicCAS(&sh.w->status, 0, 17);   /* the walk as a whole ran far too long */
                     act = 3;
                 }

@@ -132,6 +132,9 @@ typedef struct {
     fd_scratch_dev scr;
     long long max_face_pad;    /* largest face, rounded up to 16 points */
     fd_station_stats *stats;
+    /* bounds of the walk's waits in SM clock cycles (0: the built-in ones): a worker idle this long
+     * without progress, and a whole walk running this long, end the solve with a status */
+    long long wait_cycles, walk_cycles;
 } fd_station_dev;
 
 /* Request loop of a serving session.  The host publishes station records; each CTA of the

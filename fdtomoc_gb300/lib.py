@@ -142,6 +142,7 @@ def load() -> C.CDLL:
         lib.fdgpu_last_error.argtypes = [P]
         lib.fdgpu_last_error.restype = C.c_char_p
         lib.fdgpu_set_cluster.argtypes = [P, C.c_int]
+        lib.fdgpu_set_wait_limits.argtypes = [P, C.c_longlong, C.c_longlong]
         lib.fdgpu_station_from_par.argtypes = [C.c_int, C.POINTER(C.c_char_p), C.POINTER(Station), C.c_char_p,
                                                C.c_size_t, C.c_char_p, C.c_size_t]
         lib.fdgpu_solve_host.argtypes = [P, C.c_int, C.POINTER(Station), C.POINTER(C.c_float), C.c_int, C.c_int,
@@ -160,6 +161,9 @@ def load() -> C.CDLL:
                                            C.POINTER(C.c_void_p), C.c_int, C.POINTER(P)]
         lib.fdgpu_batch_run.argtypes = [P, C.c_void_p]
         lib.fdgpu_batch_stats.argtypes = [P, C.POINTER(Stats), C.c_void_p]
+        lib.fdgpu_batch_order.argtypes = [P, C.POINTER(C.c_int), C.c_void_p]
+        lib.fdgpu_batch_set_order.argtypes = [P, C.POINTER(C.c_int), C.c_void_p]
+        lib.fdgpu_batch_tune_order.argtypes = [P, C.c_void_p]
         lib.fdgpu_batch_destroy.argtypes = [P]
         lib.fdgpu_batch_destroy.restype = None
         lib.fdgpu_velocity_to_slowness.argtypes = [P, C.c_void_p, C.c_void_p, C.c_longlong, C.c_void_p]
@@ -227,6 +231,10 @@ class Context:
     def set_cluster(self, ctas_per_station: int):
         """CTAs per station in later solves (0: automatic)."""
         _check(self.lib.fdgpu_set_cluster(self.ptr, ctas_per_station))
+
+    def set_wait_limits(self, wait_cycles: int = 0, walk_cycles: int = 0):
+        """Bounds of the solver's waits in SM cycles (0: built-in); see fdgpu_set_wait_limits."""
+        _check(self.lib.fdgpu_set_wait_limits(self.ptr, C.c_longlong(wait_cycles), C.c_longlong(walk_cycles)))
 
     def close(self):
         if self.ptr:
@@ -332,6 +340,20 @@ class Batch:
         st = (Stats * self.n)()
         _check(self.lib.fdgpu_batch_stats(self.ptr, st, C.c_void_p(stream_ptr)), self.ctx.ptr)
         return [s.as_dict() for s in st]
+
+    def order(self, stream_ptr: int = 0):
+        """Launch order: the stations' indices, first launched first."""
+        o = (C.c_int * self.n)()
+        _check(self.lib.fdgpu_batch_order(self.ptr, o, C.c_void_p(stream_ptr)), self.ctx.ptr)
+        return list(o)
+
+    def set_order(self, order, stream_ptr: int = 0):
+        o = (C.c_int * self.n)(*order)
+        _check(self.lib.fdgpu_batch_set_order(self.ptr, o, C.c_void_p(stream_ptr)), self.ctx.ptr)
+
+    def tune_order(self, stream_ptr: int = 0):
+        """Longest measured solve of the last run first."""
+        _check(self.lib.fdgpu_batch_tune_order(self.ptr, C.c_void_p(stream_ptr)), self.ctx.ptr)
 
     def close(self):
         if self.ptr:

@@ -119,6 +119,14 @@ int fdgpu_solve_host(fdgpu_ctx *ctx, int n, const fdgpu_station *st, const float
  * depend on it.  No counterpart in the reference (one OpenMP thread per station). */
 int fdgpu_set_cluster(fdgpu_ctx *ctx, int ctas_per_station);
 
+/* Bounds, in SM clock cycles, of the solver's waits in later solves of this context: a warp with
+ * nothing to do for wait_cycles, or one walk (a face, or a whole sweep) running for walk_cycles,
+ * ends that station's solve with FDGPU_ESCHED (fdgpu_stats.detail 8 or 17) instead of waiting on.
+ * 0 keeps the built-in bounds (about 2 s and 66 s at the GB300's clock, far beyond any real solve).
+ * The context stays usable after such a status.  No counterpart in the reference (its loops have
+ * no waits); it exists so that a stalled schedule is reported, and so that this is testable. */
+int fdgpu_set_wait_limits(fdgpu_ctx *ctx, long long wait_cycles, long long walk_cycles);
+
 /* Same with everything already on the device: slowness (1/v, float) of a model with strides
  * (1, s_sy, s_sz), one device field per station.  Work is queued on `stream` (a cudaStream_t,
  * NULL = the context's stream); the call returns after the solve has completed. */
@@ -139,6 +147,19 @@ int fdgpu_batch_create(fdgpu_ctx *ctx, int n, const fdgpu_station *st, const flo
 int fdgpu_batch_run(fdgpu_batch *batch, void *stream);
 int fdgpu_batch_stats(fdgpu_batch *batch, fdgpu_stats *stats, void *stream);
 void fdgpu_batch_destroy(fdgpu_batch *batch);
+
+/* Launch order of a prepared batch (no counterpart in the reference, whose OpenMP loop takes par
+ * files in list order).  CTA k solves the k-th station of the order, and CTAs beyond the resident
+ * ones start as earlier ones finish, so the batch ends sooner when its longest solves start first.
+ * A new batch is ordered by grid size; fdgpu_batch_tune_order reorders it by the solve times its
+ * last run measured, longest first (an inversion loop re-solves the same stations every
+ * iteration, so one run's times predict the next run's).  fdgpu_batch_order reads the order (the
+ * caller's station indices, in launch order) and fdgpu_batch_set_order sets one, e.g. saved from an
+ * earlier process.  These copy on `stream` and wait for it: call them between runs, not while one
+ * is in flight.  The order changes which CTA solves which station, never a result. */
+int fdgpu_batch_order(fdgpu_batch *batch, int *order, void *stream);
+int fdgpu_batch_set_order(fdgpu_batch *batch, const int *order, void *stream);
+int fdgpu_batch_tune_order(fdgpu_batch *batch, void *stream);
 
 /* velocity -> slowness on the device, slow[i] = 1/v[i] as the reference rounds it (src/sphfd.c:689) */
 int fdgpu_velocity_to_slowness(fdgpu_ctx *ctx, const float *d_velocity, float *d_slowness, long long n,

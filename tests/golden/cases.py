@@ -149,3 +149,79 @@ def write_start_case(case: dict, dirname: str) -> str:
 
 
 START_SEEDS = (3, 8, 14, 27, 40, 61)
+
+
+# ---- byte-swapped models and times (par key swab, src/sphfd.c:667-686 and :5774-5795) ----------
+
+SWAB_SEEDS = (3, 8, 21)
+
+
+def write_swab_case(case: dict, dirname: str, swab: int) -> str:
+    """A random case with swab = 1, 2 or 3.  For swab 1 and 3 the model is written the way the
+    reference expects to swap it back: every header number (not the text) and every velocity
+    byte-reversed."""
+    pf = write_random_case(case, dirname)
+    if swab in (1, 3):
+        p = case["par"]
+        head = VHead(header=b"HEADFINESPHRVPMDNOFLcase", x0=p["x0"], y0=p["y0"], z0=p["z0"],
+                     nx=p["nx"], ny=p["ny"], nz=p["nz"], dz=p["h"])
+        with open(os.path.join(dirname, "vp.mod"), "wb") as f:
+            f.write(head.pack(">"))
+            f.write(np.ascontiguousarray(case["vel"], dtype=">f4").tobytes())
+    with open(pf, "a") as f:
+        f.write(f"swab={swab}\n")
+    return pf
+
+
+# ---- one inversion iteration's P and S par files (make_par_file's dialect) ---------------------
+
+def ps_station_case(dirname: str, n_sta: int = 4, seed: int = 5):
+    """P and S solves of n_sta surface stations on a shared 41x37x23 grid, written as the reference's
+    make_par_file writes them (fdtomoc_gb300.parfiles, grid size given), with VP.mod and VS.mod in
+    dirname.  Returns (par paths in parlist order, VP model, VS model)."""
+    from fdtomoc_gb300 import parfiles
+    from fdtomoc_gb300.workloads import Grid, head_for, layered_model
+    g = Grid(41, 37, 23, 0.01, 0.01, 1.0, x0=120.5, y0=23.5, z0=-2.0)
+    vp = layered_model(g, 0.05, 5.0, seed)
+    rng = np.random.default_rng(seed + 100)
+    vs = (vp / np.float32(1.73) * (1 + 0.02 * rng.uniform(-1, 1, size=vp.shape))).astype(np.float32)
+    os.makedirs(dirname, exist_ok=True)
+    write_grid(os.path.join(dirname, "VP.mod"), head_for(g), vp)
+    write_grid(os.path.join(dirname, "VS.mod"), head_for(g, b"HEADFINESPHRVSMDNOFLsynthetic"), vs)
+    # spec: the grid origin and spacing that make_par_file copies into every par file
+    spec = os.path.join(dirname, "mpf.spec")
+    with open(spec, "w") as f:
+        f.write(f"x0 {g.x0}\ny0 {g.y0}\nz0 {g.z0}\nh {g.h}\nsph 1\ntimedir ttimes\n")
+    sta = os.path.join(dirname, "stations.txt")
+    with open(sta, "w") as f:
+        for k in range(n_sta):
+            fx, fy = rng.uniform(3, g.nx - 4), rng.uniform(3, g.ny - 4)
+            elev = int(rng.integers(0, 1900))
+            lat, lon = g.y0 - fy * g.dlat, g.x0 + fx * g.dlon
+            f.write(f"{lat:.3f} {lon:.3f} {elev} ST{k:02d} {lat:.5f} {lon:.5f}\n")
+    # make_par_file names the models without a directory; these par files are read from dirname,
+    # so the velfile lines are given with it
+    paths = parfiles.make_par_files(spec, sta, dirname, nx=g.nx, ny=g.ny, nz=g.nz,
+                                    p_model=os.path.join(dirname, "VP.mod"),
+                                    s_model=os.path.join(dirname, "VS.mod"))
+    # the grid's angular spacing, which make_par_file leaves out, appended to each par file
+    for p in paths:
+        with open(p, "a") as f:
+            f.write(f"dq={g.dlat}\ndf={g.dlon}\n")
+    return paths, vp, vs
+
+
+# ---- the reference make_par_file's inputs --------------------------------------------------------
+
+PARFILE_CASES = {
+    "plain": {
+        "spec": "x0 120.9\ny0 23.8\nz0 -4.0\nh 2.0\nsph 0\ntimedir ./ttimes\n",
+        "stations": "23.12651 121.37915 0.198 M001\n22.98765 120.55555 1.234 TW02\n"
+                    "23.50000 121.00000 0.000 ABCDE\n\nIGNORED 1 2 3\n",
+    },
+    "spherical": {
+        "spec": "x0 120.25\ny0 23.75\nz0 -3.5\nh 0.25\nsph 1\ntimedir ./ttimes\n",
+        "stations": "23.126 121.379 198 M001 23.12651 121.37915\n22.988 120.556 1234 TW02 22.98765 120.55555\n"
+                    "23.5 121.0 -15 LOW 23.50000 121.00000\n",
+    },
+}

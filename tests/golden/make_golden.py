@@ -1,7 +1,7 @@
 """Generate the golden fixtures of the parity tests from the reference itself.
 
-Run in a container that has the reference sources at /root/reference (oracle/Makefile builds the
-reference's own sphfd from them into oracle/_ref/sphfd_ref):
+Run where the reference sources are present (their root from $FDTOMOC_REFERENCE; oracle/Makefile
+builds the reference's own sphfd from them into oracle/_ref/sphfd_ref):
 
     python tests/golden/make_golden.py
 
@@ -14,7 +14,10 @@ Writes:
   reference_outputs.json
                     SHA-256 of the reference binary's time file for seeded cases (cases.py), for
                     solves from a supplied start (srctype 2 and 3, fill=1; cases.start_case) and for
-                    config 1 (fdtomoc_gb300.workloads), with their sweep counts.
+                    config 1 (fdtomoc_gb300.workloads), with their sweep counts; for byte-swapped
+                    models and times (swab 1/2/3, cases.write_swab_case); and for one iteration's
+                    P and S par files in make_par_file's dialect, solved through the reference's
+                    parlist driver (cases.ps_station_case).
 """
 import hashlib
 import json
@@ -29,7 +32,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 sys.path.insert(0, HERE)
-REF = "/root/reference"
+REF = os.environ.get("FDTOMOC_REFERENCE", "/root/reference")
 REF_BIN = os.path.join(ROOT, "oracle", "_ref", "sphfd_ref")
 M001_PAR = dict(fxs="121.37915", fys="23.12651", fzs="-0.198", nx="41.000000", ny="41.000000", nz="31.000000",
                 x0="120.9", y0="23.8", z0="-4.0", h="2.0", timefile="M001.ptimes", reverse="50")
@@ -112,6 +115,29 @@ def main():
     log = run_reference(os.path.join(d, "S0000.par"), os.path.join(d, "ref"))
     b = open(os.path.join(d, "ref", "S0000.ptimes"), "rb").read()
     out["config1_S0000"] = {"sha256": hashlib.sha256(b).hexdigest(), "sweeps": sweeps_of(log)}
+    # byte-swapped models and times
+    from cases import SWAB_SEEDS, ps_station_case, write_swab_case
+    swabs = {}
+    for s in SWAB_SEEDS:
+        for sw in (1, 2, 3):
+            d = os.path.join(tmp, f"w{s}_{sw}")
+            pf = write_swab_case(random_case(s), d, sw)
+            run_reference(pf, os.path.join(d, "out"))
+            b = open(os.path.join(d, "out", "case.ptimes"), "rb").read()
+            swabs[f"{s}_{sw}"] = {"sha256": hashlib.sha256(b).hexdigest(), "bytes": len(b)}
+    out["swab_cases"] = swabs
+    # one iteration's P and S par files (make_par_file's dialect) through the reference's parlist driver
+    d = os.path.join(tmp, "ps")
+    paths, _, _ = ps_station_case(d)
+    with open(os.path.join(d, "parlist_ref"), "w") as f:
+        f.write("".join("par=" + p + "\n" for p in paths))
+    spec = os.path.join(d, "spec_ref")
+    with open(spec, "w") as f:
+        f.write(f"parlist {os.path.join(d, 'parlist_ref')}\ntimedir {os.path.join(d, 'out')}\n")
+    os.makedirs(os.path.join(d, "out"))
+    subprocess.run([REF_BIN], input=spec + "\n", capture_output=True, text=True, check=True)
+    out["ps_stations"] = {f: hashlib.sha256(open(os.path.join(d, "out", f), "rb").read()).hexdigest()
+                          for f in sorted(os.listdir(os.path.join(d, "out")))}
     json.dump(out, open(os.path.join(HERE, "reference_outputs.json"), "w"), indent=1)
     print(json.dumps({k: (v if k != "cases" else len(v)) for k, v in out.items()}))
 

@@ -125,3 +125,50 @@ def test_batch_rejects_bad_station(gpu_lib, tmp_path):
         out = torch.empty(16, dtype=torch.float32, device="cuda")
         with pytest.raises(lib.FdgpuError):
             lib.Batch(ctx, [bad], slow.data_ptr(), nx, nx * ny, [out.data_ptr()])
+
+
+def test_launch_order_tuned_by_measured_times(gpu_lib, tmp_path):
+    """fdgpu_batch_tune_order puts the longest solves of the last run first; any order gives the same
+    fields, bit for bit."""
+    import torch
+    lib = gpu_lib
+    cases = _cases(lib, tmp_path, range(1, 60))[:8]
+    st0, vel = cases[0]
+    nz, ny, nx = vel.shape
+    # windows of the first case's model with different sizes and sources
+    wins = []
+    for k in range(6):
+        w = lib.Station.from_buffer_copy(st0)
+        w.ox, w.oy, w.oz = k % 2, (k // 2) % 2, 0
+        w.nx, w.ny, w.nz = nx - w.ox - (k % 3), ny - w.oy, nz - (k % 2)
+        w.xs, w.ys, w.zs = min(st0.xs, w.nx - 1), min(st0.ys, w.ny - 1), min(st0.zs, w.nz - 1)
+        wins.append(w)
+    with lib.Context(0) as ctx:
+        slow = _slowness(ctx, vel)
+        outs = [torch.empty((w.nz, w.ny, w.nx), dtype=torch.float32, device="cuda") for w in wins]
+        b = lib.Batch(ctx, wins, slow.data_ptr(), nx, nx * ny, [o.data_ptr() for o in outs])
+        b.run()
+        first = [o.clone() for o in outs]
+        stats = b.stats()
+        dur = [s["t_end_ns"] - s["t_start_ns"] for s in stats]
+        b.tune_order()
+        order = b.order()
+        assert sorted(order) == list(range(len(wins)))
+        assert [dur[k] for k in order] == sorted(dur, reverse=True)
+        for o in outs:
+            o.fill_(-1.0)
+        b.run()
+        torch.cuda.synchronize()
+        for a, o in zip(first, outs):
+            assert torch.equal(a.view(torch.int32), o.view(torch.int32))
+        b.set_order(list(reversed(order)))
+        assert b.order() == list(reversed(order))
+        for o in outs:
+            o.fill_(-1.0)
+        b.run()
+        torch.cuda.synchronize()
+        for a, o in zip(first, outs):
+            assert torch.equal(a.view(torch.int32), o.view(torch.int32))
+        with pytest.raises(lib.FdgpuError):
+            b.set_order([0] * len(wins))
+        b.close()
