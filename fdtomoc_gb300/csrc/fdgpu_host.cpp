@@ -914,6 +914,10 @@ void run_setups(std::vector<ParSetup> &ps, std::vector<int> &stat, const char *o
             if (ctx)
                 rc = fdgpu_solve_host(ctx, (int)sts.size(), sts.data(), vel.data(), s0.nx, s0.ny, s0.nz, outp.data(),
                                       pass == 1 ? initp.data() : nullptr, sst.data());
+            /* a failed solve is reported on stderr, as the reference reports its failures */
+            if (rc)
+                std::fprintf(stderr, "sphfd: %s: %s%s%s\n", ps[sel[0]].velfile.c_str(), fdgpu_strerror(rc),
+                             ctx && *fdgpu_last_error(ctx) ? ": " : "", ctx ? fdgpu_last_error(ctx) : "");
             for (size_t j = 0; j < sel.size(); j++) {
                 if (rc) { stat[sel[j]] = rc; continue; }
                 stat[sel[j]] = write_times(ps[sel[j]], hin, out[j], output_path);

@@ -224,8 +224,10 @@ class Context:
     """An fdgpu_ctx on one device: owns geometry tables, scratch and a stream."""
 
     def __init__(self, device: int = 0):
+        import weakref
         self.lib = load()
         self.ptr = C.c_void_p()
+        self._batches = weakref.WeakSet()
         _check(self.lib.fdgpu_create(device, C.byref(self.ptr)))
 
     def set_cluster(self, ctas_per_station: int):
@@ -238,6 +240,8 @@ class Context:
 
     def close(self):
         if self.ptr:
+            for b in list(getattr(self, "_batches", ())):
+                b.close()
             self.lib.fdgpu_destroy(self.ptr)
             self.ptr = C.c_void_p()
 
@@ -332,6 +336,7 @@ class Batch:
         self.ptr = C.c_void_p()
         _check(self.lib.fdgpu_batch_create(ctx.ptr, self.n, arr, C.c_void_p(slowness_ptr), s_sy, s_sz, tp,
                                            1 if initialised else 0, C.byref(self.ptr)), ctx.ptr)
+        ctx._batches.add(self)   # a batch is destroyed before its context
 
     def run(self, stream_ptr: int = 0):
         _check(self.lib.fdgpu_batch_run(self.ptr, C.c_void_p(stream_ptr)), self.ctx.ptr)

@@ -148,6 +148,7 @@ def test_launch_order_tuned_by_measured_times(gpu_lib, tmp_path):
         outs = [torch.empty((w.nz, w.ny, w.nx), dtype=torch.float32, device="cuda") for w in wins]
         b = lib.Batch(ctx, wins, slow.data_ptr(), nx, nx * ny, [o.data_ptr() for o in outs])
         b.run()
+        torch.cuda.synchronize()
         first = [o.clone() for o in outs]
         stats = b.stats()
         dur = [s["t_end_ns"] - s["t_start_ns"] for s in stats]
