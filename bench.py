@@ -1,11 +1,13 @@
 #!/usr/bin/env python3
 """Benchmark of the GB300 sphfd travel-time solver.
 
-Metric: station travel-time fields per second (with node-updates/s), batched, on the 64-station
-201x201x81 workload (0.005 deg x 0.005 deg x 0.5 km, layered 1-D model with a 5 % / 10 km
-perturbation, seed 2; stations on the surface with 0-2 km elevation).  One step = one batch of
-64 station solves.  Every GPU field is bit-identical to the CPU oracle (checked here on the
-stations the CPU baseline solves).
+Metric: station travel-time fields per second (with node-updates/s).  Default workload: 500 station
+windows sized uniformly in 41..301 x 41..301 x 41..121 (seed 3) over a 401x401x161 model at
+0.005 deg x 0.005 deg x 0.5 km (layered 1-D model with a 5 % / 10 km perturbation, seed 4), solved as
+one prepared batch: one step = one kernel launch over all 500 windows.  Every field is compared with
+the reference binary's (SHA-256 pins made by tests/golden/make_headline_golden.py).  The same line
+carries the config-2 legs: 64 stations of 201x201x81 in one launch, and the location, c2f, ray and
+serving legs on their fields.
 
   python bench.py [--gpus N] [--steps K] [--warmup W]     GPU arm (torchrun for N > 1)
   python bench.py --impl reference ...                     CPU arm: the oracle on the host cores
@@ -46,9 +48,11 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--stations", type=int, default=None, help="stations per GPU (default 64; config 1: 1)")
     ap.add_argument("--rate", type=float, default=12.0, help="--config 4: request arrivals per second")
-    ap.add_argument("--config", type=int, default=2, choices=[1, 2, 3, 4],
-                    help="2: the benchmark workload; 1: the one-station 61x61x31 case, for profiling; "
-                         "3: the 500-window uneven batch; 4: served P/S requests (each its own JSON line)")
+    ap.add_argument("--config", type=int, default=3, choices=[1, 2, 3, 4],
+                    help="3 (default): the 500-window uneven batch, with the config-2 legs; 2: 64 stations of "
+                         "201x201x81; 1: the one-station 61x61x31 case, for profiling; 4: served P/S requests; "
+                         "5: stations on the full 401x401x161 grid with memory admission (each its own JSON line)")
+    ap.add_argument("--no-config2", action="store_true", help="--config 3: leave out the config-2 legs")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--serve-requests", type=int, default=300,
                     help="requests of the serving leg (0: skip it)")
@@ -502,47 +506,159 @@ def profile_legs(args):
     ctx.close()
 
 
-def run_config3(args):
-    """--config 3: the uneven-window batch.  500 station windows sized uniformly in 41..301 x 41..301 x
-    41..121 (seed 3) over the 401x401x161 model (seed 4), solved in one launch (largest windows
-    first), against the plain form (one window per launch, timed on a sample of windows).  Parity:
-    the sampled windows' batch fields equal their plain fields bit for bit, and the three smallest
-    windows equal the CPU oracle's fields.  Prints one JSON line."""
-    import numpy as np
-    import torch
-    from fdtomoc_gb300 import build, lib, workloads as W
+HEADLINE = os.path.join(ROOT, "tests", "golden", "headline_reference.json")
+C3_METRIC = "station fields/s (500 uneven windows in one launch, bit-identical to reference)"
+C3_WORKLOAD = "500 windows 41..301 x 41..301 x 41..121 over a 401x401x161 model, 0.005deg x 0.005deg x 0.5km (config 3)"
+CPU_WINDOW_MAX_S = 6.0   # windows in the CPU sample: at most this many oracle seconds each on the x86 build host
+
+
+def headline_fixture():
+    """Reference-binary pins of the config-2 stations and config-3 windows (make_headline_golden.py)."""
+    return json.load(open(HEADLINE)) if os.path.exists(HEADLINE) else None
+
+
+def field_sha(t) -> str:
+    import hashlib
+    return hashlib.sha256(t.cpu().numpy().tobytes()).hexdigest()
+
+
+def config3_case(rank: int):
+    """The config-3 model, this rank's windows (rank 0: the benchmark's 500; rank r > 0: its own 500,
+    seed 3 + 1000 r) and a directory with their par files."""
+    from fdtomoc_gb300 import workloads as W
     from fdtomoc_gb300.formats import write_par
     g, v, _ = W.config(3)
-    wins = W.config3_windows()
-    case_dir = tempfile.mkdtemp(prefix="fdbench_c3_")
-    W.write_case(case_dir, g, v, [])
+    wins = W.config3_windows(500, 3 + 1000 * rank)
+    case_dir = tempfile.mkdtemp(prefix=f"fdbench_c3_r{rank}_")
     velfile = os.path.join(case_dir, "vp.mod")
     pars = []
     for w in wins:
         pf = os.path.join(case_dir, w["name"] + ".par")
         write_par(pf, W.window_par(g, w, velfile, w["name"] + ".ptimes"))
         pars.append(pf)
-    # CPU oracle on the three smallest windows, before any CUDA call in this process.  sphfd reads the
-    # first nx*ny*nz values of its velocity file, so each of these windows gets its own file, cut from
-    # the model where the GPU reads its window (ox, oy, 0)
-    from fdtomoc_gb300.formats import write_grid
-    sizes = [w["nx"] * w["ny"] * w["nz"] for w in wins]
-    small = sorted(range(len(wins)), key=lambda k: sizes[k])[:3]
-    for k in small:
-        w = wins[k]
-        wg = W.Grid(w["nx"], w["ny"], w["nz"], g.dlon, g.dlat, g.h, x0=g.x0 + w["ox"] * g.dlon,
-                    y0=g.y0 - w["oy"] * g.dlat, z0=g.z0)
-        wf = os.path.join(case_dir, w["name"] + ".mod")
-        write_grid(wf, W.head_for(wg), np.ascontiguousarray(v[:w["nz"], w["oy"]:w["oy"] + w["ny"], w["ox"]:w["ox"] + w["nx"]]))
-        write_par(pars[k], W.window_par(g, w, wf, w["name"] + ".ptimes"))
-    cpu_wall, cpu_nu, cpu_out = cpu_solve(case_dir, [wins[k]["name"] for k in small], 3)
+    return g, v, wins, case_dir, pars
+
+
+def cpu_windows(g, v, wins, names, case_dir, cores):
+    """The oracle (exact pruned mode) on the named windows, one process per core, each window with its
+    own velocity file cut from the model where the GPU reads it.  Returns {name: (seconds, node
+    updates)} and the output directory."""
+    import numpy as np
+    from fdtomoc_gb300 import workloads as W
+    from fdtomoc_gb300.formats import write_grid, write_par
+    exe = build_oracle()
+    out = os.path.join(case_dir, "cpu_out")
+    os.makedirs(out, exist_ok=True)
+    by = {w["name"]: w for w in wins}
+    env = dict(os.environ, FDO_MODE="fast", OMP_NUM_THREADS="1")
+    pending, running, res = list(names), [], {}
+    while pending or running:
+        while pending and len(running) < cores:
+            nm = pending.pop(0)
+            w = by[nm]
+            wg = W.Grid(w["nx"], w["ny"], w["nz"], g.dlon, g.dlat, g.h, x0=g.x0 + w["ox"] * g.dlon,
+                        y0=g.y0 - w["oy"] * g.dlat, z0=g.z0)
+            wf = os.path.join(case_dir, nm + ".mod")
+            write_grid(wf, W.head_for(wg), np.ascontiguousarray(v[:w["nz"], w["oy"]:w["oy"] + w["ny"],
+                                                                  w["ox"]:w["ox"] + w["nx"]]))
+            pf = os.path.join(case_dir, nm + ".cpu.par")
+            write_par(pf, W.window_par(g, w, wf, nm + ".ptimes"))
+            pl = os.path.join(case_dir, f"pl_{nm}")
+            with open(pl, "w") as f:
+                f.write(f"par={pf}\n")
+            spec = os.path.join(case_dir, f"spec_{nm}")
+            with open(spec, "w") as f:
+                f.write(f"parlist {pl}\ntimedir {out}\n")
+            p = subprocess.Popen([exe], stdin=subprocess.PIPE, stdout=subprocess.DEVNULL, stderr=subprocess.PIPE,
+                                 text=True, env=env)
+            p.stdin.write(spec + "\n")
+            p.stdin.close()
+            running.append((nm, p, time.time()))
+        time.sleep(0.01)
+        still = []
+        for nm, p, t0 in running:
+            if p.poll() is None:
+                still.append((nm, p, t0))
+                continue
+            dt = time.time() - t0
+            log = p.stderr.read()
+            if p.returncode != 0:
+                raise RuntimeError(f"oracle failed on {nm}: {log}")
+            nu = 0
+            for tok in log.split():
+                if tok.startswith("node_updates="):
+                    nu = int(tok.split("=")[1])
+            res[nm] = (dt, nu)
+            os.remove(os.path.join(case_dir, nm + ".mod"))
+        running = still
+    return res, out
+
+
+def cpu_sample_names(wins, fix, cores, step):
+    """A seeded sample of `cores` windows for CPU step `step`: windows taken in a seeded permutation of
+    the 500, keeping those the oracle solved in at most CPU_WINDOW_MAX_S on the x86 build host (so a
+    step stays short), consecutive slices for consecutive steps."""
+    import numpy as np
+    perm = np.random.default_rng(31).permutation(len(wins))
+    ok = [wins[k]["name"] for k in perm
+          if fix is None or fix["config3"][wins[k]["name"]]["oracle_s"] <= CPU_WINDOW_MAX_S]
+    start = (step * cores) % max(1, len(ok) - cores + 1)
+    return ok[start:start + cores]
+
+
+def cpu_estimate(res, fix, cores):
+    """Whole-workload CPU fields/s from a sample: node updates per core-second over the sample, times
+    the cores, divided by the mean node updates of a window over all 500 windows (from the fixture)."""
+    nu = sum(x[1] for x in res.values())
+    sec = sum(x[0] for x in res.values())
+    mean_nu = (sum(x["node_updates"] for x in fix["config3"].values()) / len(fix["config3"])) if fix else nu / len(res)
+    return cores * (nu / sec) / mean_nu, nu / sec, mean_nu
+
+
+def run_config3(args):
+    """The benchmark (default): the 500 uneven windows of config 3 over the 401x401x161 model, solved
+    as one prepared batch (fdgpu_batch_*: one kernel launch per step, capturable), launch order
+    tuned by the first warm-up run's measured solve times.  Parity: every window's field is hashed and
+    compared with the reference binary's (tests/golden/headline_reference.json).  Also: the plain form
+    (one window per launch, a seeded sample), the same workload end to end through the host-buffer
+    entry point, an extrapolated CPU baseline, the roofline, and the config-2 legs (64 stations of
+    201x201x81 and the neighbours' kernels on their fields)."""
+    import numpy as np
+    rank, world, local = dist_env()
+    fix = headline_fixture() if rank == 0 else None
+    g, v, wins, case_dir, pars = config3_case(rank)
+    ncores = os.cpu_count() or 1
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        names = cpu_sample_names(wins, fix, ncores, 0)
+        t0 = time.time()
+        res, cpu_out = cpu_windows(g, v, wins, names, case_dir, ncores)
+        wall = time.time() - t0
+        est, rate, mean_nu = cpu_estimate(res, fix, ncores)
+        ora_ok = None
+        if fix:
+            ora_ok = sum(hashlib_file(os.path.join(cpu_out, nm + ".ptimes")) == fix["config3"][nm]["file_sha256"]
+                         for nm in names)
+        cpu = {"value": est, "unit": UNIT, "cores": ncores, "kind": "port",
+               "sample": f"{len(names)} seeded windows of the 500 (oracle FAST mode, one process per core, "
+                         f"{wall:.1f} s wall): {rate / 1e6:.3f} M node updates per core-second, extrapolated to "
+                         f"the workload's mean of {mean_nu / 1e6:.2f} M node updates per window",
+               "node_updates_per_s": rate * ncores, "extrapolated": True,
+               "sample_equal_reference": None if ora_ok is None else f"{ora_ok}/{len(names)}"}
+    import torch
+    from fdtomoc_gb300 import build, lib
     build.build()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     stations = []
     for w, pf in zip(wins, pars):
         st = lib.station_from_par("par=" + pf)[0]
         st.ox, st.oy, st.oz = w["ox"], w["oy"], 0
         stations.append(st)
-    ctx = lib.Context(0)
+    sizes = [w["nx"] * w["ny"] * w["nz"] for w in wins]
+    ctx = lib.Context(local)
     stream = torch.cuda.Stream()
     vel_d = torch.from_numpy(v.reshape(-1)).cuda()
     slow = torch.empty_like(vel_d)
@@ -550,29 +666,51 @@ def run_config3(args):
     stream.synchronize()
     del vel_d
     fields = [torch.empty(st.shape, dtype=torch.float32, device="cuda") for st in stations]
-    ptrs = [f.data_ptr() for f in fields]
-
-    def batch():
-        return ctx.solve_device(stations, slow.data_ptr(), g.nx, g.nx * g.ny, ptrs, stream_ptr=stream.cuda_stream)
-
-    for _ in range(max(1, args.warmup)):
-        stats = batch()
+    batch = lib.Batch(ctx, stations, slow.data_ptr(), g.nx, g.nx * g.ny, [f.data_ptr() for f in fields])
+    tuned = False
+    for k in range(args.warmup):
+        batch.run(stream.cuda_stream)
+        if k == 0:
+            batch.tune_order(stream.cuda_stream)   # longest measured solve first from here on
+            tuned = True
+    stream.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    sampler = ClockSampler(local)
+    if world > 1:
+        torch.distributed.barrier()
     torch.cuda.synchronize()
-    sampler = ClockSampler(0)
     sampler.start()
     e0.record(stream)
     for _ in range(args.steps):
-        stats = batch()
+        batch.run(stream.cuda_stream)
     e1.record(stream)
     torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
     clocks = sampler.stop()
-    ms = e0.elapsed_time(e1) / args.steps
+    ms = e0.elapsed_time(e1)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_step = ms / args.steps
+    stats = batch.stats(stream.cuda_stream)
     nu = sum(s_["node_updates"] for s_ in stats)
-    # plain: one window per launch, on a seeded sample
+    t_first = min(x["t_start_ns"] for x in stats)
+    done = sorted((s_["t_end_ns"] - t_first) / 1e6 for s_ in stats)
+    # parity: every field against the reference binary's
+    parity = None
+    if fix:
+        same = sum(field_sha(f) == fix["config3"][w["name"]]["data_sha256"] for f, w in zip(fields, wins))
+        sweeps_same = sum(s_["sweeps"] == fix["config3"][w["name"]]["sweeps"] for s_, w in zip(stats, wins))
+        model_same = hashlib_bytes(np.ascontiguousarray(v, dtype="<f4").tobytes()) == fix["models"]["config3"]
+        parity = {"windows_bit_identical_to_reference": f"{same}/{len(wins)}",
+                  "sweep_counts_equal_reference": f"{sweeps_same}/{len(wins)}", "model_equal_pinned": model_same,
+                  "against": "SHA-256 of the reference binary's time files (tests/golden/headline_reference.json)"}
+    # plain form: one window per launch, a seeded sample
     rng = np.random.default_rng(33)
     sample = [int(k) for k in rng.choice(len(wins), 8, replace=False)]
-    plain_ms, same = [], 0
+    plain_ms, plain_same = [], 0
     for k in sample:
         out = torch.empty_like(fields[k])
         e0.record(stream)
@@ -581,35 +719,180 @@ def run_config3(args):
         e1.record(stream)
         torch.cuda.synchronize()
         plain_ms.append(e0.elapsed_time(e1))
-        same += int(torch.equal(out, fields[k]))
-    # the oracle's fields of the smallest windows
-    ora_same = 0
-    for k in small:
-        ref = np.fromfile(os.path.join(cpu_out, wins[k]["name"] + ".ptimes"), dtype="<f4", offset=232)
-        ora_same += int(np.array_equal(ref, fields[k].cpu().numpy().reshape(-1)))
+        plain_same += int(torch.equal(out, fields[k]))
     plain_fps = 1e3 / (sum(plain_ms) / len(plain_ms))
+    value = len(wins) * world / (ms_step / 1e3)
+    # end to end through the host-buffer entry point: the velocity model in from pinned memory, the
+    # 500 fields out to pinned memory, every step
+    import ctypes as C
+    L = lib.load()
+    vel_h = torch.from_numpy(v.reshape(-1).copy()).pin_memory()
+    outs_h = [torch.empty(st.shape, dtype=torch.float32).pin_memory() for st in stations]
+    arr = (lib.Station * len(stations))(*stations)
+    outp = (C.POINTER(C.c_float) * len(stations))(*[C.cast(o.data_ptr(), C.POINTER(C.c_float)) for o in outs_h])
+    del fields
+    batch.close()
+    torch.cuda.synchronize()
+    t0 = time.time()
+    rc = L.fdgpu_solve_host(ctx.ptr, len(stations), arr, C.cast(vel_h.data_ptr(), C.POINTER(C.c_float)), g.nx,
+                            g.ny, g.nz, outp, None, None)
+    e2e_s = time.time() - t0
+    if rc != 0:
+        raise RuntimeError(f"fdgpu_solve_host failed: {rc}")
+    e2e_same = None
+    if fix:
+        e2e_same = sum(hashlib_bytes(o.numpy().tobytes()) == fix["config3"][w["name"]]["data_sha256"]
+                       for o, w in zip(outs_h, wins))
+    e2e = {"value": len(wins) * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(v.size * 4),
+           "d2h_bytes_per_step": int(sum(o.numel() * 4 for o in outs_h)), "steps": 1,
+           "launch_order": "largest grid first (the host entry point prepares a new batch every call)",
+           "windows_bit_identical_to_reference": None if e2e_same is None else f"{e2e_same}/{len(wins)}"}
+    del outs_h, vel_h
+    # the config-2 legs: 64 stations of 201x201x81 in one launch, and the neighbours on their fields
+    c2 = config2_legs(args, lib, ctx, stream, fix) if rank == 0 and not args.no_config2 else None
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    peak = peaks.get("hbm_gbs", 6800.0)
+    achieved = ALGO_BYTES_PER_NODE_UPDATE * nu / (ms_step / 1e3) / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "fd_solve_traffic.json")
+    if os.path.exists(tpath):
+        traffic = json.load(open(tpath))["dram_bytes_per_node_update"] * nu
+    st_sum = [sum(s_["stencils"][k] for s_ in stats) for k in range(5)]
+    fp64_ops = 116 * st_sum[0] + 70 * st_sum[1] + 69 * st_sum[2] + 25 * st_sum[3] + 6 * st_sum[4]
+    fp64_peak = ctx.probe_fp64_gops()
+    if rank == 0:
+        line = {
+            "metric": C3_METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64 stencils / f32 fields", "data": "synthetic (seeded, config 3 recipe)",
+            "config": {"workload": C3_WORKLOAD, "windows_per_gpu": len(wins), "nodes_per_gpu": int(sum(sizes)),
+                       "launch": "one prepared batch (fdgpu_batch_run), one kernel per step",
+                       "launch_order": "longest measured solve first (tuned on the first warm-up run)" if tuned
+                       else "largest grid first",
+                       "l2": "inputs larger than L2 (500 fields, 4.7 GB, + 104 MB model)",
+                       "parallelism": f"windows x{world}"},
+            "node_updates_per_s": nu * world / (ms_step / 1e3),
+            "latency_ms": {"p50": done[len(done) // 2], "p99": done[min(len(done) - 1, int(round(0.99 * (len(done) - 1))))],
+                           "what": "window completion time within the step"},
+            "plain": {"sample_windows": len(sample), "ms_per_window_mean": sum(plain_ms) / len(plain_ms),
+                      "fields_per_s": plain_fps, "batched_over_plain": value / world / plain_fps,
+                      "sample_equal_batch": f"{plain_same}/{len(sample)}"},
+            "e2e": e2e,
+            "gpu_launches": args.steps,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": traffic, "peak_kind": "of measured (MEASURED_PEAKS.json hbm_gbs)",
+                         "note": "the path is bound by FP64 issue and dependency latency, not HBM"},
+            "fp64": {"achieved_gops": fp64_ops / (ms_step / 1e3) / 1e9, "peak_gops": fp64_peak,
+                     "frac": fp64_ops / (ms_step / 1e3) / 1e9 / fp64_peak,
+                     "peak_kind": "measured live (FP64 fused multiply-add chains, all SMs)"},
+            "parity": parity,
+            "clocks": clocks,
+        }
+        if cpu is not None:
+            line["cpu_baseline"] = cpu
+        if c2 is not None:
+            line["config2"] = c2
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    shutil.rmtree(case_dir, ignore_errors=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def hashlib_bytes(b: bytes) -> str:
+    import hashlib
+    return hashlib.sha256(b).hexdigest()
+
+
+def hashlib_file(path: str) -> str:
+    return hashlib_bytes(open(path, "rb").read()[232:])
+
+
+def config2_legs(args, lib, ctx, stream, fix):
+    """64 stations of config 2 in one launch (timed once, fields hashed against the reference's), then
+    the location, c2f, ray and serving legs on those fields."""
+    import torch
+    g, v, sts = workload(0, STATIONS_PER_GPU, 2)
+    case_dir = tempfile.mkdtemp(prefix="fdbench_c2_")
+    write_case(case_dir, g, v, sts)
+    stations = [lib.station_from_par("par=" + os.path.join(case_dir, s["name"] + ".par"))[0] for s in sts]
+    vel_d = torch.from_numpy(v.reshape(-1)).cuda()
+    slow = torch.empty_like(vel_d)
+    ctx.velocity_to_slowness(vel_d.data_ptr(), slow.data_ptr(), v.size, stream.cuda_stream)
+    fields = [torch.empty(s.shape, dtype=torch.float32, device="cuda") for s in stations]
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    stats = ctx.solve_device(stations, slow.data_ptr(), g.nx, g.nx * g.ny, [f.data_ptr() for f in fields],
+                             stream_ptr=stream.cuda_stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    out = {"workload": CONFIG_NAME, "fields_per_s": len(stations) / (ms / 1e3), "ms_per_step": ms,
+           "node_updates_per_s": sum(s_["node_updates"] for s_ in stats) / (ms / 1e3), "steps": 1}
+    if fix:
+        same = sum(field_sha(f) == fix["config2"][s["name"]]["data_sha256"] for f, s in zip(fields, sts))
+        out["stations_bit_identical_to_reference"] = f"{same}/{len(sts)}"
+    # one station alone: the latency of a single 201x201x81 solve
+    e0.record(stream)
+    ctx.solve_device(stations[:1], slow.data_ptr(), g.nx, g.nx * g.ny, [fields[0].data_ptr()],
+                     stream_ptr=stream.cuda_stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    out["single_station_ms"] = e0.elapsed_time(e1)
+    if args.locate_events > 0:
+        out["locate"] = locate_leg(args, lib, ctx, g, fields, stream)
+    if not args.no_c2f:
+        out["c2f"] = c2f_leg(args, lib, ctx, stream)
+    if args.ray_events > 0:
+        out["rays"] = ray_leg(args, lib, ctx, g, sts, fields, stream)
+    profiled = bool(os.environ.get("CUDA_INJECTION64_PATH"))
+    if args.serve_requests > 0 and not profiled:
+        out["serving"] = serve_leg(args, lib, stations, v, fields)
+    shutil.rmtree(case_dir, ignore_errors=True)
+    return out
+
+
+def run_reference_config3(args):
+    """Reference arm on the config-3 workload: the CPU restatement of the reference's solver (oracle/,
+    pinned bit for bit against the reference binary; the reference's own sources do not exist on the
+    GPU host) on all host cores, one process per core as the reference's OpenMP driver runs par files.
+    Each step solves a seeded sample of one window per core (consecutive slices of a seeded
+    permutation, windows of at most CPU_WINDOW_MAX_S oracle seconds so that a step stays short); the
+    reported fields/s extrapolates the node updates per core-second to the workload's mean window."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    fix = headline_fixture()
+    g, v, wins, case_dir, _ = config3_case(0)
+    ncores = os.cpu_count() or 1
+    for k in range(args.warmup):
+        cpu_windows(g, v, wins, cpu_sample_names(wins, fix, ncores, 1000 + k)[:1], case_dir, 1)
+    res_all, walls = {}, []
+    for k in range(args.steps):
+        t0 = time.time()
+        res, _ = cpu_windows(g, v, wins, cpu_sample_names(wins, fix, ncores, k), case_dir, ncores)
+        walls.append(time.time() - t0)
+        res_all.update({f"{k}:{n}": x for n, x in res.items()})
+    est, rate, mean_nu = cpu_estimate(res_all, fix, ncores)
     line = {
-        "metric": "station fields/s (batched uneven windows, bit-identical to reference)", "value": len(wins) / (ms / 1e3),
-        "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": max(1, args.warmup), "ms_per_step": ms,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64 stencils / f32 fields",
+        "impl": "reference", "metric": C3_METRIC, "value": est, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * sum(walls) / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64 stencils / f32 fields",
         "data": "synthetic (seeded, config 3 recipe)",
-        "config": {"workload": "500 windows 41..301 x 41..301 x 41..121 over a 401x401x161 model (config 3)",
-                   "windows": len(wins), "nodes": int(sum(sizes)), "launch_order": "largest windows first"},
-        "node_updates_per_s": nu / (ms / 1e3),
-        "latency_ms": {"p50": float(np.percentile([(s_["t_end_ns"] - min(x["t_start_ns"] for x in stats)) / 1e6 for s_ in stats], 50)),
-                       "p99": float(np.percentile([(s_["t_end_ns"] - min(x["t_start_ns"] for x in stats)) / 1e6 for s_ in stats], 99)),
-                       "what": "window completion time within the batch"},
-        "plain": {"sample_windows": len(sample), "ms_per_window_mean": sum(plain_ms) / len(plain_ms),
-                  "fields_per_s": plain_fps, "batched_over_plain": len(wins) / (ms / 1e3) / plain_fps},
-        "parity": {"sampled_windows_batch_equals_plain": f"{same}/{len(sample)}",
-                   "smallest_windows_equal_oracle": f"{ora_same}/{len(small)}"},
-        "cpu_baseline": {"value": len(small) / cpu_wall, "unit": UNIT, "cores": 3, "kind": "port",
-                         "sample": f"the {len(small)} smallest windows, one oracle process each (oracle FAST mode)"},
-        "clocks": clocks,
-        "gpu_launches": args.steps,
+        "config": {"workload": C3_WORKLOAD, "parallelism": f"{ncores} processes x 1 thread"},
+        "node_updates_per_s": rate * ncores,
+        "cpu_baseline": {"value": est, "unit": UNIT, "cores": ncores, "kind": "port", "extrapolated": True,
+                         "sample": f"{ncores} seeded windows per step (oracle FAST mode, exact), "
+                                   f"{rate / 1e6:.3f} M node updates per core-second, extrapolated to the workload's "
+                                   f"mean of {mean_nu / 1e6:.2f} M node updates per window"},
+        "e2e": {"value": est, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
-    ctx.close()
     shutil.rmtree(case_dir, ignore_errors=True)
 
 
@@ -936,7 +1219,9 @@ def main():
     args = parse()
     if args.profile_legs:
         profile_legs(args)
-    elif args.config == 3 and args.impl != "reference":
+    elif args.config == 3 and args.impl == "reference":
+        run_reference_config3(args)
+    elif args.config == 3:
         run_config3(args)
     elif args.config == 4 and args.impl != "reference":
         run_config4(args)

@@ -16,6 +16,8 @@
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <mutex>
+#include <thread>
 #include <memory>
 #include <string>
 #include <tuple>
@@ -856,22 +858,48 @@ int write_times(const ParSetup &ps, const VHead &hin, std::vector<float> &t, con
     return ok ? FDGPU_OK : FDGPU_EIO;
 }
 
-/* per-thread context of the drop-in entry points; deliberately never destroyed, so no CUDA call
- * runs during process teardown */
-fdgpu_ctx *default_ctx(int *status)
+/* Contexts of the drop-in entry points' worker threads, one per (device, position in the device
+ * list), created on first use.  Like the per-thread ones below they are deliberately never
+ * destroyed, so that no CUDA call runs during process teardown.  Calls that use several devices
+ * must not overlap: their workers share these contexts. */
+fdgpu_ctx *slot_ctx(int device, int slot, int *status)
 {
-    thread_local fdgpu_ctx *ctx = nullptr;
+    static std::mutex mu;
+    static std::map<std::pair<int, int>, fdgpu_ctx *> ctxs;
+    std::lock_guard<std::mutex> lk(mu);
+    fdgpu_ctx *&ctx = ctxs[{device, slot}];
     if (!ctx) {
-        *status = fdgpu_create(0, &ctx);
+        *status = fdgpu_create(device, &ctx);
         if (*status) ctx = nullptr;
     }
     return ctx;
 }
 
+/* the calling thread's own context on a device (the single-device drop-in: concurrent callers on
+ * different threads do not share one) */
+fdgpu_ctx *thread_ctx(int device, int *status)
+{
+    thread_local std::map<int, fdgpu_ctx *> ctxs;
+    fdgpu_ctx *&ctx = ctxs[device];
+    if (!ctx) {
+        *status = fdgpu_create(device, &ctx);
+        if (*status) ctx = nullptr;
+    }
+    return ctx;
+}
+
+/* the calling thread's current device (the one a caller selected with cudaSetDevice; 0 if none) */
+int current_device()
+{
+    int d = 0;
+    return cudaGetDevice(&d) == cudaSuccess ? d : 0;
+}
+
 /* solve a set of parsed par files and write their time files.  Every input (par file, velocity
  * file, starting field) is read and checked before the GPU is touched: the context is created on
  * the first solve, so a run whose inputs are all bad returns their statuses without a device. */
-void run_setups(std::vector<ParSetup> &ps, std::vector<int> &stat, const char *output_path)
+void run_setups(std::vector<ParSetup> &ps, std::vector<int> &stat, const char *output_path,
+                const std::vector<int> &devices)
 {
     const int n = (int)ps.size();
     /* group stations by velocity file and grid so each model is read and uploaded once */
@@ -908,19 +936,38 @@ void run_setups(std::vector<ParSetup> &ps, std::vector<int> &stat, const char *o
                 }
             }
             if (bad) { for (int k : sel) if (!stat[k]) stat[k] = FDGPU_EIO; continue; }
-            std::vector<fdgpu_stats> sst(sel.size());
-            const fdgpu_station &s0 = sts[0];
-            fdgpu_ctx *ctx = default_ctx(&rc);
-            if (ctx)
-                rc = fdgpu_solve_host(ctx, (int)sts.size(), sts.data(), vel.data(), s0.nx, s0.ny, s0.nz, outp.data(),
-                                      pass == 1 ? initp.data() : nullptr, sst.data());
-            /* a failed solve is reported on stderr, as the reference reports its failures */
-            if (rc)
-                std::fprintf(stderr, "sphfd: %s: %s%s%s\n", ps[sel[0]].velfile.c_str(), fdgpu_strerror(rc),
-                             ctx && *fdgpu_last_error(ctx) ? ": " : "", ctx ? fdgpu_last_error(ctx) : "");
-            for (size_t j = 0; j < sel.size(); j++) {
-                if (rc) { stat[sel[j]] = rc; continue; }
-                stat[sel[j]] = write_times(ps[sel[j]], hin, out[j], output_path);
+            /* the stations of this group, dealt round-robin over the devices; one worker thread per
+             * device with more than one, each with its own context */
+            const int nd = (int)std::min(devices.size(), sts.size());
+            auto work = [&](int d) {
+                std::vector<int> mine;
+                for (size_t j = d; j < sel.size(); j += nd) mine.push_back((int)j);
+                std::vector<fdgpu_station> ms;
+                std::vector<float *> mo;
+                std::vector<const float *> mi;
+                for (int j : mine) {
+                    ms.push_back(sts[j]);
+                    mo.push_back(outp[j]);
+                    if (pass == 1) mi.push_back(initp[j]);
+                }
+                std::vector<fdgpu_stats> sst(ms.size());
+                int rcd = FDGPU_OK;
+                fdgpu_ctx *ctx = nd > 1 ? slot_ctx(devices[d], d, &rcd) : thread_ctx(devices[d], &rcd);
+                if (ctx)
+                    rcd = fdgpu_solve_host(ctx, (int)ms.size(), ms.data(), vel.data(), ms[0].nx, ms[0].ny, ms[0].nz,
+                                           mo.data(), pass == 1 ? mi.data() : nullptr, sst.data());
+                /* a failed solve is reported on stderr, as the reference reports its failures */
+                if (rcd)
+                    std::fprintf(stderr, "sphfd: %s: %s%s%s\n", ps[sel[0]].velfile.c_str(), fdgpu_strerror(rcd),
+                                 ctx && *fdgpu_last_error(ctx) ? ": " : "", ctx ? fdgpu_last_error(ctx) : "");
+                for (int j : mine) stat[sel[j]] = rcd ? rcd : write_times(ps[sel[j]], hin, out[j], output_path);
+            };
+            if (nd <= 1) {
+                work(0);
+            } else {
+                std::vector<std::thread> th;
+                for (int d = 0; d < nd; d++) th.emplace_back(work, d);
+                for (auto &t : th) t.join();
             }
         }
     }
@@ -941,16 +988,22 @@ extern "C" int fdgpu_station_from_par(int ac, char **av, fdgpu_station *st, char
     return FDGPU_OK;
 }
 
-extern "C" int fdgpu_sphfd_parlist(int n, char **entries, const char *output_path, int *status)
+extern "C" int fdgpu_sphfd_parlist_devices(int n, char **entries, const char *output_path, int *status, int ndev,
+                                           const int *devices)
 {
-    if (n < 0 || (n > 0 && !entries) || !output_path) return FDGPU_EINVAL;
+    if (n < 0 || (n > 0 && !entries) || !output_path || ndev < 1 || !devices) return FDGPU_EINVAL;
+    std::vector<int> devs(devices, devices + ndev);
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess) count = 0;
+    for (int d : devs)
+        if (d < 0 || (count > 0 && d >= count)) return FDGPU_ENODEV;
     std::vector<ParSetup> ps(n);
     std::vector<int> stat(n, FDGPU_OK);
     for (int k = 0; k < n; k++) {
         char *av[2] = {(char *)"sphfd", entries[k]};
         stat[k] = setup_from_par(2, av, ps[k]);
     }
-    run_setups(ps, stat, output_path);
+    run_setups(ps, stat, output_path, devs);
     int first = FDGPU_OK;
     for (int k = 0; k < n; k++) {
         if (status) status[k] = stat[k];
@@ -959,11 +1012,17 @@ extern "C" int fdgpu_sphfd_parlist(int n, char **entries, const char *output_pat
     return first;
 }
 
+extern "C" int fdgpu_sphfd_parlist(int n, char **entries, const char *output_path, int *status)
+{
+    const int dev = current_device();
+    return fdgpu_sphfd_parlist_devices(n, entries, output_path, status, 1, &dev);
+}
+
 extern "C" int fdgpu_sphfd(int ac, char **av, const char *output_path)
 {
     if (ac < 1 || !av || !output_path) return FDGPU_EINVAL;
     std::vector<ParSetup> ps(1);
     std::vector<int> stat(1, setup_from_par(ac, av, ps[0]));
-    run_setups(ps, stat, output_path);
+    run_setups(ps, stat, output_path, {current_device()});
     return stat[0];
 }

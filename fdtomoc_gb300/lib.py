@@ -228,6 +228,7 @@ class Context:
         self.lib = load()
         self.ptr = C.c_void_p()
         self._batches = weakref.WeakSet()
+        self.device = device
         _check(self.lib.fdgpu_create(device, C.byref(self.ptr)))
 
     def set_cluster(self, ctas_per_station: int):
@@ -459,13 +460,20 @@ class C2fPlan:
             pass
 
 
-def sphfd_parlist(entries, timedir: str):
-    """Drop-in for the reference's main loop: entries like "par=/path/sta.par"; returns statuses."""
+def sphfd_parlist(entries, timedir: str, devices=None):
+    """Drop-in for the reference's main loop: entries like "par=/path/sta.par"; returns statuses.
+    devices: a list of GPUs to deal the stations over (default: the current device)."""
     lib = load()
     n = len(entries)
     argv = (C.c_char_p * n)(*[e.encode() for e in entries])
     status = (C.c_int * n)()
-    lib.fdgpu_sphfd_parlist(n, argv, timedir.encode(), status)
+    if devices:
+        dv = (C.c_int * len(devices))(*devices)
+        rc = lib.fdgpu_sphfd_parlist_devices(n, argv, timedir.encode(), status, len(devices), dv)
+        if rc == -8:
+            raise FdgpuError("fdgpu error -8 (ENODEV): a listed device does not exist")
+    else:
+        lib.fdgpu_sphfd_parlist(n, argv, timedir.encode(), status)
     return list(status)
 
 

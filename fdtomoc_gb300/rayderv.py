@@ -385,10 +385,13 @@ def default_cap(grid: RayGrid) -> int:
     return 8 * (grid.nx + grid.ny + grid.nz) + 64
 
 
-def run(specfile: str, trace, cap: int | None = None, spacing_rule: bool = True) -> dict[str, bytes]:
+def run(specfile: str, trace, cap: int | None = None, spacing_rule: bool = True,
+        write: bool | None = None) -> dict[str, bytes]:
     """sphrayderv on one spec: trace(grid, fields, obs, nobs, cap) -> (results, off, idx, du) does
-    the rays (fields as host arrays); returns the file contents by spec name (and writes them where
-    the spec says).  spacing_rule: as grid_from_spec."""
+    the rays (fields as host arrays); returns the file contents by spec name and writes them where
+    the spec says.  spacing_rule: as grid_from_spec.  write: None writes unless `trace` is a sharded
+    tracer on a rank other than 0 (ranks that share a file system then do not write the same files
+    at once); every rank returns the contents."""
     sp = read_spec(specfile)
     if sp["ivpvs"] or sp["dotel"] or sp["doshot"] or sp["nomat"]:
         raise ValueError("only local earthquakes with ivpvs 0 and nomat 0 are supported")
@@ -404,16 +407,23 @@ def run(specfile: str, trace, cap: int | None = None, spacing_rule: bool = True)
     for inside, rows in plan:
         asm.event(inside, rows, results, off, idx, du)
     out = asm.files()
-    for name, data in out.items():
-        with open(sp[name], "wb") as fh:
-            fh.write(data)
+    if write is None:
+        writer = getattr(trace, "writes", None)
+        write = writer() if writer else True
+    if write:
+        for name, data in out.items():
+            with open(sp[name], "wb") as fh:
+                fh.write(data)
     del keep
     return out
 
 
-def gpu_trace(ctx=None, device: int = 0):
-    """A tracer for run(): the fields go to the device and fdgpu_raytrace traces the rays."""
+def gpu_trace(ctx=None, device: int | None = None):
+    """A tracer for run(): the fields go to the device and fdgpu_raytrace traces the rays.  The device
+    defaults to $LOCAL_RANK (0 when unset), so that each rank of a sharded run uses its own GPU."""
     from . import lib as L
+    if device is None:
+        device = ctx.device if ctx is not None and hasattr(ctx, "device") else int(os.environ.get("LOCAL_RANK", 0))
 
     def trace(grid, fields, obs, nobs, cap):
         import torch
@@ -456,4 +466,9 @@ def sharded(trace, group=None):
         np.cumsum([all_res[o].nnz for o in range(nobs)], out=off_all[1:])
         return all_res, off_all, idx_all, du_all
 
+    def writes():
+        import torch.distributed as dist
+        return dist.get_rank(group) == 0
+
+    run.writes = writes
     return run

@@ -447,15 +447,28 @@ typedef int (*fdgpu_ray_tracer)(void *user, const fdgpu_ray_grid *g, const float
  * refused with FDGPU_EINVAL. */
 int fdgpu_sphrayderv(const char *specfile, int spacing_rule, fdgpu_ray_tracer tracer, void *user);
 
-/* Drop-in sphfd(): ac/av as the reference's (av[1] = "par=<file>"), output_path = timedir.
- * Reads the velocity file, solves on the GPU, writes <output_path>/<timefile> byte-for-byte as
- * the reference does.  Uses a per-thread default context on device 0. */
+/* Drop-in sphfd() (src/sphfd.c:260): ac/av as the reference's (av[1] = "par=<file>"),
+ * output_path = timedir.  Reads the velocity file, solves on the GPU, writes
+ * <output_path>/<timefile> byte-for-byte as the reference does.  Inputs are read and checked before
+ * the GPU is touched; the solve runs on the calling thread's current device (cudaSetDevice; 0 by
+ * default) in a context of that thread, created on first use. */
 int fdgpu_sphfd(int ac, char **av, const char *output_path);
 
-/* Drop-in for main()'s loop over a par list: every entry is "par=<file>"; all stations are solved
- * together (stations sharing a velocity file share one device copy).  status[k] receives each
- * station's result if status is non-NULL; the return value is the first failure (or 0). */
+/* Drop-in for main()'s OpenMP loop over a par list (src/sphfd.c:231-255): every entry is
+ * "par=<file>"; all stations are solved together (stations sharing a velocity file share one read
+ * of it and one device copy).  status[k] receives each station's result if status is non-NULL; the
+ * return value is the first failure (or 0).  Runs on the calling thread's current device. */
 int fdgpu_sphfd_parlist(int n, char **par_entries, const char *output_path, int *status);
+
+/* The same over several GPUs of this process: the stations of each velocity-file group are dealt
+ * round-robin over devices[0..ndev) (a device may be listed twice: two contexts share it), solved
+ * by one worker thread per listed device, and written by the workers (each station to its own
+ * file).  The velocity file is read once per group on the host.  Stations are independent, so the
+ * files equal the single-device ones byte for byte.  The reference's counterpart is its OpenMP
+ * parallel loop over par files (src/sphfd.c:247-255), one thread per station.  Calls of this
+ * function must not overlap. */
+int fdgpu_sphfd_parlist_devices(int n, char **par_entries, const char *output_path, int *status, int ndev,
+                                const int *devices);
 
 #ifdef __cplusplus
 }
