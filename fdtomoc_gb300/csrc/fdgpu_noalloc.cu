@@ -15,7 +15,12 @@
  *
  * Set-up: the first call on a device looks up the array's device address with
  * cudaGetSymbolAddress (host code cannot use the array's name as a device pointer) and caches it
- * for that device.  Make that first call before any stream capture on the device.
+ * for that device.  Make that first call before any stream capture on the device.  The cached
+ * address belongs to the device's primary context: after cudaDeviceReset it is stale, and the
+ * entry point must not be called again in that process.
+ *
+ * Device: the call works on the calling thread's current device; a stream of another device is
+ * refused with FDGPU_EINVAL before any work is queued.
  *
  * Sharing: every call uses the same array, so two calls that overlap on one GPU (for example from
  * two host threads on two streams) corrupt each other's scratch.  Callers must serialise calls per
@@ -111,6 +116,11 @@ extern "C" int fdgpu_solve_noalloc(const fdgpu_station *st, const float *d_slown
 
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return FDGPU_ENODEV;
+    if (stream) {
+        int sdev = -1;
+        if (cudaStreamGetDevice(static_cast<cudaStream_t>(stream), &sdev) != cudaSuccess || sdev != dev)
+            return FDGPU_EINVAL;
+    }
     unsigned char *base = nullptr;
     rc = scratch_address(dev, &base);
     if (rc) return rc;

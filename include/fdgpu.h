@@ -179,10 +179,13 @@ int fdgpu_probe_fp64(fdgpu_ctx *ctx, double *gops);
  * statistics, geometry tables, face-walk scratch) lives in one static device array of
  * FDGPU_NOALLOC_SCRATCH_BYTES per GPU, held from library load to process exit.  A station that needs
  * more returns FDGPU_ETOOBIG before any GPU work; a 201x201x81 grid needs about 12 MiB.  The first
- * call on a device looks up the array's address; make it before any stream capture.  Calls share the
- * array, so calls that overlap on one GPU race: serialise them per device.  The call returns when the
- * solve has finished on `stream` (a cudaStream_t, NULL = default stream); results are bit-identical
- * to fdgpu_solve_device. */
+ * call on a device looks up the array's address; make it before any stream capture.  That address
+ * is kept for the life of the process: it does not survive cudaDeviceReset (or any other teardown
+ * of the device's primary context), after which this entry point must not be called again.  The
+ * call runs on the calling thread's current device, and `stream` (a cudaStream_t, NULL = the
+ * default stream) must belong to that device (FDGPU_EINVAL otherwise).  Calls share the array, so
+ * calls that overlap on one GPU race: serialise them per device.  The call returns when the solve
+ * has finished on `stream`; results are bit-identical to fdgpu_solve_device. */
 #define FDGPU_NOALLOC_SCRATCH_BYTES (16u << 20)
 int fdgpu_solve_noalloc(const fdgpu_station *st, const float *d_slowness, long long s_sy, long long s_sz,
                         float *d_time, fdgpu_stats *stats, void *stream);
