@@ -637,7 +637,7 @@ def run_config3(args):
         est, rate, mean_nu = cpu_estimate(res, fix, ncores)
         ora_ok = None
         if fix:
-            ora_ok = sum(hashlib_file(os.path.join(cpu_out, nm + ".ptimes")) == fix["config3"][nm]["file_sha256"]
+            ora_ok = sum(hashlib_file(os.path.join(cpu_out, nm + ".ptimes")) == fix["config3"][nm]["data_sha256"]
                          for nm in names)
         cpu = {"value": est, "unit": UNIT, "cores": ncores, "kind": "port",
                "sample": f"{len(names)} seeded windows of the 500 (oracle FAST mode, one process per core, "
@@ -745,7 +745,7 @@ def run_config3(args):
                        for o, w in zip(outs_h, wins))
     e2e = {"value": len(wins) * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(v.size * 4),
            "d2h_bytes_per_step": int(sum(o.numel() * 4 for o in outs_h)), "steps": 1,
-           "launch_order": "largest grid first (the host entry point prepares a new batch every call)",
+           "launch_order": "longest measured solve first (the context's order table, filled by the batch's runs)",
            "windows_bit_identical_to_reference": None if e2e_same is None else f"{e2e_same}/{len(wins)}"}
     del outs_h, vel_h
     # the config-2 legs: 64 stations of 201x201x81 in one launch, and the neighbours on their fields

@@ -91,6 +91,9 @@ struct fdgpu_ctx {
     int device = 0;
     int cluster = 0;   /* CTAs per station: 0 automatic */
     long long wait_cycles = 0, walk_cycles = 0;   /* bounds of the solver's waits, 0: built-in */
+    /* measured solve time (ns) of each station this context has solved, keyed by the station's
+     * record (fdgpu_station bytes): the launch-order table */
+    std::map<std::string, long long> solve_ns;
     cudaStream_t stream = nullptr;
     std::map<GeoKey, std::unique_ptr<Geo>> geos;
     BatchBufs batch;   /* the buffers of fdgpu_solve_device, kept for the next call */
@@ -252,6 +255,54 @@ extern "C" int fdgpu_set_cluster(fdgpu_ctx *ctx, int ctas_per_station)
     return FDGPU_OK;
 }
 
+/* the launch-order table on disk: "FDGPUORD", a record count, then per station its key length,
+ * key and solve time (ns), all little-endian as written by this machine */
+extern "C" int fdgpu_order_save(const fdgpu_ctx *ctx, const char *path)
+{
+    if (!ctx || !path) return FDGPU_EINVAL;
+    FILE *fp = std::fopen(path, "wb");
+    if (!fp) return FDGPU_EIO;
+    bool ok = std::fwrite("FDGPUORD", 1, 8, fp) == 8;
+    const long long n = (long long)ctx->solve_ns.size();
+    ok = ok && std::fwrite(&n, sizeof n, 1, fp) == 1;
+    for (const auto &kv : ctx->solve_ns) {
+        const int len = (int)kv.first.size();
+        ok = ok && std::fwrite(&len, sizeof len, 1, fp) == 1 && std::fwrite(kv.first.data(), 1, len, fp) == (size_t)len
+             && std::fwrite(&kv.second, sizeof kv.second, 1, fp) == 1;
+    }
+    ok = std::fclose(fp) == 0 && ok;
+    return ok ? FDGPU_OK : FDGPU_EIO;
+}
+
+extern "C" int fdgpu_order_load(fdgpu_ctx *ctx, const char *path)
+{
+    if (!ctx || !path) return FDGPU_EINVAL;
+    FILE *fp = std::fopen(path, "rb");
+    if (!fp) return FDGPU_EIO;
+    char magic[8];
+    long long n = 0;
+    int rc = FDGPU_OK;
+    if (std::fread(magic, 1, 8, fp) != 8 || std::memcmp(magic, "FDGPUORD", 8) != 0 || std::fread(&n, sizeof n, 1, fp) != 1
+        || n < 0 || n > (1ll << 24))
+        rc = FDGPU_EIO;
+    std::map<std::string, long long> got;
+    for (long long k = 0; rc == FDGPU_OK && k < n; k++) {
+        int len = 0;
+        long long ns = 0;
+        if (std::fread(&len, sizeof len, 1, fp) != 1 || len <= 0 || len > 4096) { rc = FDGPU_EIO; break; }
+        std::string key((size_t)len, '\0');
+        if (std::fread(&key[0], 1, (size_t)len, fp) != (size_t)len || std::fread(&ns, sizeof ns, 1, fp) != 1) {
+            rc = FDGPU_EIO;
+            break;
+        }
+        got[key] = ns;
+    }
+    std::fclose(fp);
+    if (rc == FDGPU_OK)
+        for (auto &kv : got) ctx->solve_ns[kv.first] = kv.second;
+    return rc;
+}
+
 extern "C" int fdgpu_set_wait_limits(fdgpu_ctx *ctx, long long wait_cycles, long long walk_cycles)
 {
     if (!ctx || wait_cycles < 0 || walk_cycles < 0) return FDGPU_EINVAL;
@@ -261,6 +312,20 @@ extern "C" int fdgpu_set_wait_limits(fdgpu_ctx *ctx, long long wait_cycles, long
 }
 
 namespace {
+
+/* a station's key in the launch-order table: its fields' bytes, member by member (the struct's
+ * padding is not part of it) */
+std::string station_key(const fdgpu_station &s)
+{
+    std::string k;
+    auto put = [&k](const void *p, size_t n) { k.append(reinterpret_cast<const char *>(p), n); };
+    const int iv[] = {s.nx, s.ny, s.nz, s.srctype, s.xs, s.ys, s.zs, s.ncube, s.reverse, s.headpref, s.maxrad,
+                      s.kminus, s.kplus, s.iplus, s.iminus, s.jminus, s.jplus, s.srcwall, s.ox, s.oy, s.oz};
+    const double dv[] = {s.h, s.dq, s.df, s.x0, s.y0, s.z0r, s.src_geo[0], s.src_geo[1], s.src_geo[2]};
+    put(iv, sizeof iv);
+    put(dv, sizeof dv);
+    return k;
+}
 
 /* Check the stations and lay out their records in bufs (queued on cs): everything a launch of
  * fd_solve reads, except the fields and the slowness it points at.  *max_pad: the largest face. */
@@ -306,9 +371,23 @@ int prepare_batch(fdgpu_ctx *ctx, int n, const fdgpu_station *st, const float *s
      * start as earlier ones finish, so a batch of uneven windows ends sooner when the long solves
      * start first (longest-processing-time order).  Each record keeps its own statistics slot, so
      * the caller's order is unaffected. */
-    std::stable_sort(hs.begin(), hs.end(), [](const fd_station_dev &a, const fd_station_dev &b) {
-        return (long long)a.g.nx * a.g.ny * a.g.nz > (long long)b.g.nx * b.g.ny * b.g.nz;
-    });
+    std::vector<long long> known(n, -1);
+    bool all_known = true;
+    for (int k = 0; k < n; k++) {
+        auto it = ctx->solve_ns.find(station_key(st[k]));
+        if (it != ctx->solve_ns.end()) known[k] = it->second; else all_known = false;
+    }
+    if (all_known) {
+        /* every station has a measured solve time in this context: longest first */
+        const fd_station_stats *sbase = bufs.stats.as<fd_station_stats>();
+        std::stable_sort(hs.begin(), hs.end(), [&](const fd_station_dev &a, const fd_station_dev &b) {
+            return known[a.stats - sbase] > known[b.stats - sbase];
+        });
+    } else {
+        std::stable_sort(hs.begin(), hs.end(), [](const fd_station_dev &a, const fd_station_dev &b) {
+            return (long long)a.g.nx * a.g.ny * a.g.nz > (long long)b.g.nx * b.g.ny * b.g.nz;
+        });
+    }
     FD_CU(ctx, cudaMemcpyAsync(bufs.trig.p, trig.data(), sizeof(double) * trig.size(), cudaMemcpyHostToDevice, cs));
     FD_CU(ctx, cudaMemcpyAsync(bufs.stations.p, hs.data(), sizeof(fd_station_dev) * n, cudaMemcpyHostToDevice, cs));
     /* the host vectors go away on return: the copies must have left them */
@@ -317,8 +396,11 @@ int prepare_batch(fdgpu_ctx *ctx, int n, const fdgpu_station *st, const float *s
     return FDGPU_OK;
 }
 
-/* the public statistics of n solves from their device records (queued on cs, then waited for) */
-int read_stats(fdgpu_ctx *ctx, const DevBuf &stats_buf, int n, fdgpu_stats *stats, cudaStream_t cs)
+/* The public statistics of n solves from their device records (queued on cs, then waited for).
+ * Clean solves' times go into the context's launch-order table (st: the stations, in the caller's
+ * order). */
+int read_stats(fdgpu_ctx *ctx, const DevBuf &stats_buf, int n, fdgpu_stats *stats, cudaStream_t cs,
+               const fdgpu_station *st)
 {
     std::vector<fd_station_stats> hst(n);
     FD_CU(ctx, cudaMemcpyAsync(hst.data(), stats_buf.p, sizeof(fd_station_stats) * n, cudaMemcpyDeviceToHost, cs));
@@ -327,6 +409,8 @@ int read_stats(fdgpu_ctx *ctx, const DevBuf &stats_buf, int n, fdgpu_stats *stat
     for (int k = 0; k < n; k++) {
         if (stats) fdh::copy_stats(stats[k], hst[k]);
         if (hst[k].status && rc == FDGPU_OK) rc = FDGPU_ESCHED;
+        if (st && !hst[k].status && hst[k].t_end_ns > hst[k].t_start_ns)
+            ctx->solve_ns[station_key(st[k])] = hst[k].t_end_ns - hst[k].t_start_ns;
     }
     return rc;
 }
@@ -336,6 +420,7 @@ int read_stats(fdgpu_ctx *ctx, const DevBuf &stats_buf, int n, fdgpu_stats *stat
 struct fdgpu_batch {
     fdgpu_ctx *ctx = nullptr;
     int n = 0;
+    std::vector<fdgpu_station> stations;   /* the caller's stations, in its order */
     long long max_pad = 16;
     long long smem_bytes = 0;   /* launch shape, fixed at creation */
     int csz = 1;
@@ -355,7 +440,7 @@ extern "C" int fdgpu_solve_device(fdgpu_ctx *ctx, int n, const fdgpu_station *st
     int rc = prepare_batch(ctx, n, st, slowness, s_sy, s_sz, d_times, times_initialised, bufs, cs, &max_pad);
     if (rc == FDGPU_OK) {
         const cudaError_t e = fdk_launch_solve(bufs.stations.as<fd_station_dev>(), n, max_pad, ctx->cluster, cs);
-        rc = e ? cuda_fail(ctx, e, "fdk_launch_solve") : read_stats(ctx, bufs.stats, n, stats, cs);
+        rc = e ? cuda_fail(ctx, e, "fdk_launch_solve") : read_stats(ctx, bufs.stats, n, stats, cs, st);
     }
     return rc;
 }
@@ -372,6 +457,7 @@ extern "C" int fdgpu_batch_create(fdgpu_ctx *ctx, int n, const fdgpu_station *st
     if (!b) return FDGPU_ENOMEM;
     b->ctx = ctx;
     b->n = n;
+    b->stations.assign(st, st + n);
     int rc = prepare_batch(ctx, n, st, slowness, s_sy, s_sz, d_times, times_initialised, b->bufs, ctx->stream,
                            &b->max_pad);
     if (!rc) {
@@ -399,7 +485,8 @@ extern "C" int fdgpu_batch_stats(fdgpu_batch *b, fdgpu_stats *stats, void *strea
 {
     if (!b) return FDGPU_EINVAL;
     fdgpu_ctx *ctx = b->ctx;
-    return read_stats(ctx, b->bufs.stats, b->n, stats, stream ? (cudaStream_t)stream : ctx->stream);
+    return read_stats(ctx, b->bufs.stats, b->n, stats, stream ? (cudaStream_t)stream : ctx->stream,
+                      b->stations.data());
 }
 
 namespace {

@@ -162,6 +162,8 @@ def load() -> C.CDLL:
         lib.fdgpu_batch_run.argtypes = [P, C.c_void_p]
         lib.fdgpu_batch_stats.argtypes = [P, C.POINTER(Stats), C.c_void_p]
         lib.fdgpu_batch_order.argtypes = [P, C.POINTER(C.c_int), C.c_void_p]
+        lib.fdgpu_order_save.argtypes = [P, C.c_char_p]
+        lib.fdgpu_order_load.argtypes = [P, C.c_char_p]
         lib.fdgpu_batch_set_order.argtypes = [P, C.POINTER(C.c_int), C.c_void_p]
         lib.fdgpu_batch_tune_order.argtypes = [P, C.c_void_p]
         lib.fdgpu_batch_destroy.argtypes = [P]
@@ -234,6 +236,14 @@ class Context:
     def set_cluster(self, ctas_per_station: int):
         """CTAs per station in later solves (0: automatic)."""
         _check(self.lib.fdgpu_set_cluster(self.ptr, ctas_per_station))
+
+    def save_order(self, path: str):
+        """Write the context's measured solve times (the launch-order table) to a file."""
+        _check(self.lib.fdgpu_order_save(self.ptr, path.encode()), self.ptr)
+
+    def load_order(self, path: str):
+        """Merge a saved launch-order table into the context."""
+        _check(self.lib.fdgpu_order_load(self.ptr, path.encode()), self.ptr)
 
     def set_wait_limits(self, wait_cycles: int = 0, walk_cycles: int = 0):
         """Bounds of the solver's waits in SM cycles (0: built-in); see fdgpu_set_wait_limits."""

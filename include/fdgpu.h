@@ -158,6 +158,15 @@ void fdgpu_batch_destroy(fdgpu_batch *batch);
  * earlier process.  These copy on `stream` and wait for it: call them between runs, not while one
  * is in flight.  The order changes which CTA solves which station, never a result. */
 int fdgpu_batch_order(fdgpu_batch *batch, int *order, void *stream);
+
+/* The context's launch-order table: every clean solve of fdgpu_solve_device / fdgpu_solve_host /
+ * fdgpu_batch_stats records each station's measured solve time, and a later batch whose stations all
+ * have one is launched longest first (otherwise largest grid first).  order_save writes the table to
+ * a file and order_load merges one into the context, so that a new process (the next inversion
+ * iteration, say) starts with the order the last one measured.  Results never depend on it.  No
+ * counterpart in the reference. */
+int fdgpu_order_save(const fdgpu_ctx *ctx, const char *path);
+int fdgpu_order_load(fdgpu_ctx *ctx, const char *path);
 int fdgpu_batch_set_order(fdgpu_batch *batch, const int *order, void *stream);
 int fdgpu_batch_tune_order(fdgpu_batch *batch, void *stream);
 

@@ -173,3 +173,42 @@ def test_launch_order_tuned_by_measured_times(gpu_lib, tmp_path):
         with pytest.raises(lib.FdgpuError):
             b.set_order([0] * len(wins))
         b.close()
+
+
+def test_order_table_saved_and_loaded(gpu_lib, tmp_path):
+    """A context records each solve's measured time; saved and loaded into a new context, the table
+    orders a new batch of the same stations longest first; the fields are unchanged."""
+    import torch
+    lib = gpu_lib
+    st0, vel = _cases(lib, tmp_path, range(1, 60))[0]
+    nz, ny, nx = vel.shape
+    wins = []
+    for k in range(5):
+        w = lib.Station.from_buffer_copy(st0)
+        w.ox, w.oy = k % 2, (k // 2) % 2
+        w.nx, w.ny, w.nz = nx - w.ox - (k % 3), ny - w.oy, nz - (k % 2)
+        w.xs, w.ys, w.zs = min(st0.xs, w.nx - 1), min(st0.ys, w.ny - 1), min(st0.zs, w.nz - 1)
+        wins.append(w)
+    table = str(tmp_path / "order.bin")
+    with lib.Context(0) as ctx:
+        slow = _slowness(ctx, vel)
+        outs = [torch.empty((w.nz, w.ny, w.nx), dtype=torch.float32, device="cuda") for w in wins]
+        stats = ctx.solve_device(wins, slow.data_ptr(), nx, nx * ny, [o.data_ptr() for o in outs])
+        torch.cuda.synchronize()
+        first = [o.clone() for o in outs]
+        ctx.save_order(table)
+    dur = [s["t_end_ns"] - s["t_start_ns"] for s in stats]
+    with lib.Context(0) as ctx:
+        ctx.load_order(table)
+        slow = _slowness(ctx, vel)
+        b = lib.Batch(ctx, wins, slow.data_ptr(), nx, nx * ny, [o.data_ptr() for o in outs])
+        assert [dur[k] for k in b.order()] == sorted(dur, reverse=True)
+        for o in outs:
+            o.fill_(-1.0)
+        b.run()
+        torch.cuda.synchronize()
+        for a, o in zip(first, outs):
+            assert torch.equal(a.view(torch.int32), o.view(torch.int32))
+        b.close()
+        with pytest.raises(lib.FdgpuError):
+            ctx.load_order(str(tmp_path / "missing.bin"))
