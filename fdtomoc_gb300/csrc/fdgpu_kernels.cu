@@ -272,9 +272,25 @@ __device__ __forceinline__ unsigned long long block_max_u64(unsigned long long x
     return sh.bcast;
 }
 
+/* stencil evaluations by kind (3-D, new-edge, 2-D, new-face, 1-D): the warp's counts in its
+ * shared area, passed by value (a pointer), so that no per-thread memory is involved */
 struct Counters {
-    unsigned long long n[5];
+    unsigned long long *n;
 };
+
+__device__ __forceinline__ void count_eval(Counters cn, int kind) { atomicAdd(&cn.n[kind], 1ull); }
+
+/* coordinate of node (x,y,z) along a grid axis, and a node placed from face coordinates: selects on
+ * registers (arrays indexed by a run-time axis would live in per-thread local memory, whose L1 lines
+ * this kernel's large shared-memory carve-out leaves little room for) */
+__device__ __forceinline__ int coord(int axis, int x, int y, int z) { return axis == 0 ? x : axis == 1 ? y : z; }
+
+__device__ __forceinline__ void place(const fdn_frame &fr, int u, int v, int n, int &x, int &y, int &z)
+{
+    x = fr.axis_u == 0 ? u : fr.axis_v == 0 ? v : n;
+    y = fr.axis_u == 1 ? u : fr.axis_v == 1 ? v : n;
+    z = fr.axis_u == 2 ? u : fr.axis_v == 2 ? v : n;
+}
 
 /* ---------------------------------------------------------------------------------------------- */
 /* warp workers                                                                                    */
@@ -329,6 +345,7 @@ struct WarpSmem {
     float s0[32], s4[32];                  /* stencil state entering the 2-D block */
     int z[32], y[32];                      /* grid z and y of the node */
     unsigned short items[FDN_NTRIAL * 32]; /* (slot << 5 | trial) to evaluate, trial-major */
+    unsigned long long cnt[6];             /* stencil evaluations by kind (5 used) */
 };
 static_assert(sizeof(WarpSmem) % 16 == 0, "keeps the dependency bytes after the warp areas aligned");
 constexpr int kSmemBase = kCtaSmemBytes + FD_WARPS * (int)sizeof(WarpSmem);
@@ -475,7 +492,7 @@ __device__ __forceinline__ int push_items(unsigned short *items, int n, unsigned
 
 /* evaluate items[0..n) with the warp's lanes; a 2-D value is stored after the causality selection
  * against its floor, which includes the stencil state entering the 2-D block (src/sphfd.c:6116-6121) */
-__device__ void eval_items(const fd_station_dev &sd, const TrialDesc *dsc, WarpSmem &ws, int n, int lane, Counters &cn)
+__device__ void eval_items(const fd_station_dev &sd, const TrialDesc *dsc, WarpSmem &ws, int n, int lane, Counters cn)
 {
     for (int j = lane; j < n; j += 32) {
         const unsigned it = ws.items[j];
@@ -506,7 +523,7 @@ __device__ void eval_items(const fd_station_dev &sd, const TrialDesc *dsc, WarpS
         default: v = eval_1d(d, t18, s18, sd.g, z, y); break;
         }
         ws.res[slot][K] = v;
-        cn.n[kind]++;
+        count_eval(cn, kind);
     }
 }
 
@@ -602,7 +619,7 @@ __device__ __forceinline__ long long s_stride(const fd_station_dev &sd, int a) {
 /* where a node sits: grid index, coordinates, face rectangle, fill index */
 struct Where {
     long long p;
-    int xyz[3];
+    int x, y, z;
     int i;       /* fill index in its face (instance) */
     int inst;    /* face instance of a sweep graph, -1 in a face walk */
     Rect r;
@@ -723,8 +740,7 @@ __device__ void relation_masks(int f, unsigned &ctx, unsigned &inn)
     inn = 0;
     for (int k = 0; k < 27; k++) {
         if (k == 13) continue;
-        const int o[3] = {k % 3 - 1, (k / 3) % 3 - 1, k / 9 - 1};
-        const int on = o[fr.axis_n];
+        const int on = coord(fr.axis_n, k % 3 - 1, (k / 3) % 3 - 1, k / 9 - 1);
         if (on == 0 || on == fr.inner) ctx |= 1u << k;
         if (on == fr.inner) inn |= 1u << k;
     }
@@ -735,29 +751,43 @@ __device__ __forceinline__ int rect_n(const GRect &r) { return r.nuf * (r.vhi - 
 /* owner word of node (x,y,z), which must lie in the grid */
 __device__ __forceinline__ int owner_of(const GraphSmem &gs, unsigned faces, int x, int y, int z)
 {
-    const int c[3] = {x, y, z};
 #pragma unroll
     for (int f = 0; f < 6; f++) {
         if (!((faces >> f) & 1u)) continue;
         const fdn_frame fr = frame_of(f);
-        const int I = gs.lay2inst[f][c[fr.axis_n]];
+        const int I = gs.lay2inst[f][coord(fr.axis_n, x, y, z)];
         if (I < 0) continue;
         const GRect &r = gs.rect[I];
-        const int u = c[fr.axis_u], v = c[fr.axis_v];
+        const int u = coord(fr.axis_u, x, y, z), v = coord(fr.axis_v, x, y, z);
         if (u >= r.ulo && u <= r.uhi && v >= r.vlo && v <= r.vhi) return (f << 24) | I;
     }
     return -1;
+}
+
+/* owner word of node (x,y,z) when face F is the likely owner: F's instance at the node's layer is
+ * looked at first (one table entry and one rectangle), the full search only if it is not F's.  Each
+ * node belongs to at most one instance of a sweep, so the answer is owner_of's. */
+__device__ __forceinline__ int owner_near(const GraphSmem &gs, unsigned faces, int F, int x, int y, int z)
+{
+    const fdn_frame fr = frame_of(F);
+    if ((faces >> F) & 1u) {
+        const int I = gs.lay2inst[F][coord(fr.axis_n, x, y, z)];
+        if (I >= 0) {
+            const GRect &r = gs.rect[I];
+            const int u = coord(fr.axis_u, x, y, z), v = coord(fr.axis_v, x, y, z);
+            if (u >= r.ulo && u <= r.uhi && v >= r.vlo && v <= r.vhi) return (F << 24) | I;
+        }
+    }
+    return owner_of(gs, faces, x, y, z);
 }
 
 /* node index of point j of instance r */
 __device__ __forceinline__ long long inst_node(const fd_station_dev &sd, const GRect &r, int j)
 {
     const fdn_frame fr = frame_of(r.face);
-    int xyz[3];
-    xyz[fr.axis_u] = r.ulo + j % r.nuf;
-    xyz[fr.axis_v] = r.vlo + j / r.nuf;
-    xyz[fr.axis_n] = r.layer;
-    return ((long long)xyz[2] * sd.g.ny + xyz[1]) * sd.g.nx + xyz[0];
+    int x, y, z;
+    place(fr, r.ulo + j % r.nuf, r.vlo + j / r.nuf, r.layer, x, y, z);
+    return ((long long)z * sd.g.ny + y) * sd.g.nx + x;
 }
 
 /* sort key of point j of instance r: time of its inner-layer node, then fill index */
@@ -768,11 +798,11 @@ __device__ __forceinline__ unsigned long long inst_key(const fd_station_dev &sd,
     return node_key(vload(sd.T[p]), j);
 }
 
-/* fill index of node xyz in instance r */
-__device__ __forceinline__ int inst_fill(const GRect &r, const int xyz[3])
+/* fill index of node (x,y,z) in instance r */
+__device__ __forceinline__ int inst_fill(const GRect &r, int x, int y, int z)
 {
     const fdn_frame fr = frame_of(r.face);
-    return (xyz[fr.axis_v] - r.vlo) * r.nuf + (xyz[fr.axis_u] - r.ulo);
+    return (coord(fr.axis_v, x, y, z) - r.vlo) * r.nuf + (coord(fr.axis_u, x, y, z) - r.ulo);
 }
 
 /* points parked on instance I's event `kind` (1: all keys final, 2: all done) go to the resume queue */
@@ -839,22 +869,22 @@ __device__ __forceinline__ void graph_ready(const fd_station_dev &sd, Shared &sh
 
 /* drop one inner-block (inner) or other-instance dependency of node q (instance oq, face fq) */
 __device__ __forceinline__ void graph_dec(const fd_station_dev &sd, Shared &sh, long long q, int oq, int fq,
-                                          const int qxyz[3], bool inner)
+                                          int qx, int qy, int qz, bool inner)
 {
     const unsigned dec = inner ? 1u : (1u << 16);
     if (!FD_OK(q, (long long)sd.g.nx * sd.g.ny * sd.g.nz, 19)) return;
     const unsigned nw = atomicSub(&sd.scr.gcnt[q], dec) - dec;
     if (inner && (nw & 0xFFu) == 0u) {
         /* q's inner block is complete: its key and in-face order are now known */
-        if (ready_word(key_event(sd, sh, oq, inst_fill(gsmem(sh).rect[oq], qxyz), q))) graph_ready(sd, sh, fq, q);
+        if (ready_word(key_event(sd, sh, oq, inst_fill(gsmem(sh).rect[oq], qx, qy, qz), q))) graph_ready(sd, sh, fq, q);
     } else if (ready_word(nw)) {
         graph_ready(sd, sh, fq, q);
     }
 }
 
 /* node p (instance I, face F, fill index i) is final: record, release what waits on it */
-__device__ void graph_release(const fd_station_dev &sd, Shared &sh, int F, long long p, const int pxyz[3], int I, int i,
-                              bool writer, float st0, float st4, float tin)
+__device__ void graph_release(const fd_station_dev &sd, Shared &sh, int F, long long p, int x, int y, int z, int I,
+                              int i, bool writer, float st0, float st4, float tin)
 {
     const GraphSmem &gs = gsmem(sh);
     if (!FD_OK(p, (long long)sd.g.nx * sd.g.ny * sd.g.nz, 15) || !FD_OK(I, sd.scr.ginst_cap, 16)) return;
@@ -880,25 +910,20 @@ __device__ void graph_release(const fd_station_dev &sd, Shared &sh, int F, long 
                 enqueue_to(sd.scr.grq, sh.w->rqtail, sh.w->rqcap, sh, vload(sd.scr.gwait[k].y));
     }
     const int nx = sd.g.nx, ny = sd.g.ny;
-    const int x = pxyz[0], y = pxyz[1], z = pxyz[2];
     const fdn_frame fr = frame_of(F);
     if (sh.single) {
         /* one face: the next instance's nodes whose inner block holds p */
         if (I + 1 < sh.ninst && gs.rect[I + 1].layer == r.layer - fr.inner) {
             const GRect &rn = gs.rect[I + 1];
-            int c[3] = {x, y, z};
-            c[fr.axis_n] = rn.layer;
-            const int u0 = c[fr.axis_u], v0 = c[fr.axis_v];
+            const int u0 = coord(fr.axis_u, x, y, z), v0 = coord(fr.axis_v, x, y, z);
             for (int dv = -1; dv <= 1; dv++)
                 for (int du = -1; du <= 1; du++) {
                     const int u = u0 + du, v = v0 + dv;
                     if (u < rn.ulo || u > rn.uhi || v < rn.vlo || v > rn.vhi) continue;
-                    int qxyz[3];
-                    qxyz[fr.axis_u] = u;
-                    qxyz[fr.axis_v] = v;
-                    qxyz[fr.axis_n] = rn.layer;
-                    const long long q = ((long long)qxyz[2] * ny + qxyz[1]) * nx + qxyz[0];
-                    graph_dec(sd, sh, q, I + 1, F, qxyz, true);
+                    int qx, qy, qz;
+                    place(fr, u, v, rn.layer, qx, qy, qz);
+                    const long long q = ((long long)qz * ny + qy) * nx + qx;
+                    graph_dec(sd, sh, q, I + 1, F, qx, qy, qz, true);
                 }
         }
     } else {
@@ -906,15 +931,14 @@ __device__ void graph_release(const fd_station_dev &sd, Shared &sh, int F, long 
         const unsigned myctx = sh.ctxm[F];
         for (int k = 0; k < 27; k++) {
             if (k == 13) continue;
-            const int qxyz[3] = {x + k % 3 - 1, y + (k / 3) % 3 - 1, z + k / 9 - 1};
-            if (qxyz[0] < 0 || qxyz[0] >= nx || qxyz[1] < 0 || qxyz[1] >= ny || qxyz[2] < 0 || qxyz[2] >= sd.g.nz)
-                continue;
-            const int w = owner_of(gs, sh.gfaces, qxyz[0], qxyz[1], qxyz[2]);
+            const int qx = x + k % 3 - 1, qy = y + (k / 3) % 3 - 1, qz = z + k / 9 - 1;
+            if (qx < 0 || qx >= nx || qy < 0 || qy >= ny || qz < 0 || qz >= sd.g.nz) continue;
+            const int w = owner_near(gs, sh.gfaces, F, qx, qy, qz);
             if (w < 0 || own_inst(w) <= I) continue;
             const int fq = own_face(w);
             if (!((myctx >> k) & 1u) && !((sh.ctxm[fq] >> (26 - k)) & 1u)) continue;
-            const long long q = ((long long)qxyz[2] * ny + qxyz[1]) * nx + qxyz[0];
-            graph_dec(sd, sh, q, own_inst(w), fq, qxyz, (sh.innm[fq] >> (26 - k)) & 1u);
+            const long long q = ((long long)qz * ny + qy) * nx + qx;
+            graph_dec(sd, sh, q, own_inst(w), fq, qx, qy, qz, (sh.innm[fq] >> (26 - k)) & 1u);
         }
     }
     /* later neighbours in the same instance */
@@ -984,7 +1008,7 @@ __device__ bool wait_point(const fd_station_dev &sd, Shared &sh, int w, long lon
  * returns false without committing. */
 __device__ bool commit_node(const fd_station_dev &sd, Shared &sh, const TrialDesc *dsc, WarpSmem &ws, int slot,
                             int F, const Where &wh, unsigned gm, unsigned em, float it0, float it4, bool permissive,
-                            unsigned char *dag, Counters &cn)
+                            unsigned char *dag, Counters cn)
 {
     const float *t18 = ws.t[slot], *s18 = ws.s[slot];
     const double told = f2d(t18[NB_POINT]);
@@ -1017,7 +1041,7 @@ __device__ bool commit_node(const fd_station_dev &sd, Shared &sh, const TrialDes
                 for (int k = 1; k < 5; k++) fl = fmaxf(fl, t18[d.slot[k]]);
                 if (prunable(fl, guess)) continue;
                 v = (K == TK_NF) ? eval_nf(d, t18, s18, sd.g, z, y) : eval_ne(d, t18, s18, sd.g, z, y);
-                cn.n[K == TK_NF ? 3 : 1]++;
+                count_eval(cn, K == TK_NF ? 3 : 1);
             } else {
                 continue;
             }
@@ -1041,7 +1065,7 @@ __device__ bool commit_node(const fd_station_dev &sd, Shared &sh, const TrialDes
         }
     }
     if (sh.graph)
-        graph_release(sd, sh, F, wh.p, wh.xyz, wh.inst, wh.i, writers != 0, st0, st4, t18[13]);
+        graph_release(sd, sh, F, wh.p, wh.x, wh.y, wh.z, wh.inst, wh.i, writers != 0, st0, st4, t18[13]);
     else
         face_release(sd, sh, dag, wh.i, writers != 0, st0, st4);
     return true;
@@ -1057,30 +1081,28 @@ __device__ __forceinline__ Where locate(const fd_station_dev &sd, const Shared &
     if (sh.graph) {
         wh.p = e;
         const int nx = sd.g.nx, ny = sd.g.ny, exy = e / nx;
-        wh.xyz[0] = e - exy * nx;
-        wh.xyz[2] = exy / ny;
-        wh.xyz[1] = exy - wh.xyz[2] * ny;
-        const int w = owner_of(gsmem(sh), sh.gfaces, wh.xyz[0], wh.xyz[1], wh.xyz[2]);
+        wh.x = e - exy * nx;
+        wh.z = exy / ny;
+        wh.y = exy - wh.z * ny;
+        const int w = owner_near(gsmem(sh), sh.gfaces, F, wh.x, wh.y, wh.z);
         if (w < 0) {
             ok = false;
             return wh;
         }
         wh.inst = own_inst(w);
         const GRect &gr = gsmem(sh).rect[wh.inst];
-        wh.r.u = wh.xyz[fr.axis_u];
-        wh.r.v = wh.xyz[fr.axis_v];
+        wh.r.u = coord(fr.axis_u, wh.x, wh.y, wh.z);
+        wh.r.v = coord(fr.axis_v, wh.x, wh.y, wh.z);
         wh.r.ulo = gr.ulo; wh.r.uhi = gr.uhi; wh.r.vlo = gr.vlo; wh.r.vhi = gr.vhi;
-        wh.i = inst_fill(gr, wh.xyz);
+        wh.i = inst_fill(gr, wh.x, wh.y, wh.z);
     } else {
         wh.i = e;
         wh.inst = -1;
         wh.r.u = sh.ulo + e % sh.nuf;
         wh.r.v = sh.vlo + e / sh.nuf;
         wh.r.ulo = sh.ulo; wh.r.uhi = sh.uhi; wh.r.vlo = sh.vlo; wh.r.vhi = sh.vhi;
-        wh.xyz[fr.axis_u] = wh.r.u;
-        wh.xyz[fr.axis_v] = wh.r.v;
-        wh.xyz[fr.axis_n] = sh.layer;
-        wh.p = ((long long)wh.xyz[2] * sd.g.ny + wh.xyz[1]) * sd.g.nx + wh.xyz[0];
+        place(fr, wh.r.u, wh.r.v, sh.layer, wh.x, wh.y, wh.z);
+        wh.p = ((long long)wh.z * sd.g.ny + wh.y) * sd.g.nx + wh.x;
     }
     wh.r.nu = axis_len(sd, fr.axis_u);
     wh.r.nv = axis_len(sd, fr.axis_v);
@@ -1090,7 +1112,7 @@ __device__ __forceinline__ Where locate(const fd_station_dev &sd, const Shared &
 /* Evaluate and commit one chunk of face F: lane l holds queue entry e (-1 for none).  A node given
  * with have_inherit uses (it0, it4) as the stencil state entering it.  All 32 lanes call. */
 __device__ void warp_chunk(const fd_station_dev &sd, Shared &sh, const CtaSmem &cs, WarpSmem &ws, int F, int e,
-                           bool have_inherit, float it0, float it4, unsigned char *dag, Counters &cn)
+                           bool have_inherit, float it0, float it4, unsigned char *dag, Counters cn)
 {
     const int lane = threadIdx.x & 31;
     const fdn_frame fr = frame_of(F);
@@ -1109,9 +1131,9 @@ __device__ void warp_chunk(const fd_station_dev &sd, Shared &sh, const CtaSmem &
     }
     const bool valid = e >= 0;
     if (valid) {
-        const long long pS = (long long)wh.xyz[2] * sd.s_sz + (long long)wh.xyz[1] * sd.s_sy + wh.xyz[0];
-        ws.z[lane] = wh.xyz[2];
-        ws.y[lane] = wh.xyz[1];
+        const long long pS = (long long)wh.z * sd.s_sz + (long long)wh.y * sd.s_sy + wh.x;
+        ws.z[lane] = wh.z;
+        ws.y[lane] = wh.y;
         float *tr = ws.t[lane], *sr = ws.s[lane];
         const long long su = t_stride(sd, fr.axis_u), sv = t_stride(sd, fr.axis_v);
         const long long ssu = s_stride(sd, fr.axis_u), ssv = s_stride(sd, fr.axis_v);
@@ -1222,7 +1244,7 @@ __device__ int predecessor(const fd_station_dev &sd, int n, int c, int lane)
  * next pending point).  Before the face's first point the state is the one the face started with.
  * Keys fall along the walk, so waits cannot form a cycle.  One warp; evaluates w when found. */
 __device__ void resume_waiter(const fd_station_dev &sd, Shared &sh, const CtaSmem &cs, WarpSmem &ws, int w,
-                              unsigned char *dag, Counters &cn)
+                              unsigned char *dag, Counters cn)
 {
     const int lane = threadIdx.x & 31;
     int c = w;
@@ -1265,15 +1287,15 @@ __device__ void resume_waiter(const fd_station_dev &sd, Shared &sh, const CtaSme
  * instances and, within one, of keys.  Registers w on an instance event or a point when the
  * answer is not yet known.  One warp; evaluates w when found. */
 __device__ void resume_graph(const fd_station_dev &sd, Shared &sh, const CtaSmem &cs, WarpSmem &ws, int w,
-                             Counters &cn)
+                             Counters cn)
 {
     const int lane = threadIdx.x & 31;
     const GraphSmem &gs = gsmem(sh);
     const int nx = sd.g.nx, ny = sd.g.ny;
     if (!FD_OK(w, (long long)sd.g.nx * sd.g.ny * sd.g.nz, 20)) return;
     const int wxy = w / nx;
-    const int xyz[3] = {w - wxy * nx, wxy % ny, wxy / ny};
-    const int ow = owner_of(gs, sh.gfaces, xyz[0], xyz[1], xyz[2]);
+    const int wx = w - wxy * nx, wy = wxy % ny, wz = wxy / ny;
+    const int ow = owner_of(gs, sh.gfaces, wx, wy, wz);
     if (ow < 0) {
         if (lane == 0) atomicCAS(&sh.w->status, 0, 14);
         return;
@@ -1285,7 +1307,7 @@ __device__ void resume_graph(const fd_station_dev &sd, Shared &sh, const CtaSmem
         if (lane == 0) wait_event(sd, sh, w, I, 1);
         return;
     }
-    unsigned long long kc = inst_key(sd, r, inst_fill(r, xyz));
+    unsigned long long kc = inst_key(sd, r, inst_fill(r, wx, wy, wz));
     for (int guard = 0; guard <= 2 * n + 2; guard++) {
         /* predecessor in the instance */
         unsigned long long best = 0ull;
@@ -1375,7 +1397,7 @@ __device__ __forceinline__ int read_entry(const int *queue, int pos, Shared &sh)
 
 /* the worker loop of one walk over `total` nodes; all warps call it between two CTA barriers */
 __device__ void run_walk(const fd_station_dev &sd, Shared &sh, const CtaSmem &cs, WarpSmem &ws, int total,
-                         unsigned char *dag, Counters &cn)
+                         unsigned char *dag, Counters cn)
 {
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
@@ -1494,7 +1516,7 @@ __device__ void walk_reset(Shared &sh, int nq, int rqcap)
 
 /* Walk the current face (parameters in sh) in dependency order. */
 __device__ void face_walk(const fd_station_dev &sd, Shared &sh, CtaSmem &cs, WarpSmem &ws, unsigned char *dag,
-                          Counters &cn)
+                          Counters cn)
 {
     const int n = sh.n, nuf = sh.nuf, nvf = n / nuf;
     const int tid = threadIdx.x;
@@ -1505,11 +1527,9 @@ __device__ void face_walk(const fd_station_dev &sd, Shared &sh, CtaSmem &cs, War
     FD_TIC(t0);
     /* keys: time of the inner-layer neighbour, then fill index */
     for (int i = tid; i < n; i += blockDim.x) {
-        int xyz[3];
-        xyz[fr.axis_u] = sh.ulo + i % nuf;
-        xyz[fr.axis_v] = sh.vlo + i / nuf;
-        xyz[fr.axis_n] = sh.layer + fr.inner;
-        const float tin = T[((long long)xyz[2] * sd.g.ny + xyz[1]) * sd.g.nx + xyz[0]];
+        int x, y, z;
+        place(fr, sh.ulo + i % nuf, sh.vlo + i / nuf, sh.layer + fr.inner, x, y, z);
+        const float tin = T[((long long)z * sd.g.ny + y) * sd.g.nx + x];
         sd.scr.key[i] = ((unsigned long long)okey32(tin) << 32) | (unsigned)i;
         sd.scr.pst[i] = -1;
         queue[i] = -1;
@@ -1590,7 +1610,7 @@ __device__ void setup_face(const fd_station_dev &sd, Shared &sh, int face)
 
 /* One sweep (the radius loop of src/sphfd.c:1018-5566) as one dependency graph.  Leaves walls,
  * flags, radius and the stencil-state carry as the radius loop would. */
-__device__ void graph_sweep(const fd_station_dev &sd, Shared &sh, CtaSmem &cs, WarpSmem &ws, Counters &cn)
+__device__ void graph_sweep(const fd_station_dev &sd, Shared &sh, CtaSmem &cs, WarpSmem &ws, Counters cn)
 {
     const int tid = threadIdx.x;
     /* the station's threads over all its CTAs, for loops over nodes */
@@ -1709,7 +1729,7 @@ __device__ void graph_sweep(const fd_station_dev &sd, Shared &sh, CtaSmem &cs, W
                         if (k == 13) continue;
                         const int qx = x + k % 3 - 1, qy = y + (k / 3) % 3 - 1, qz = z + k / 9 - 1;
                         if (qx < 0 || qx >= nx || qy < 0 || qy >= ny || qz < 0 || qz >= nz) continue;
-                        const int w = owner_of(gs, sh.gfaces, qx, qy, qz);
+                        const int w = owner_near(gs, sh.gfaces, r.face, qx, qy, qz);
                         if (w < 0 || own_inst(w) > I) continue;
                         if (own_inst(w) == I) { c2++; continue; }
                         if (!((myctx >> k) & 1u) && !((sh.ctxm[own_face(w)] >> (26 - k)) & 1u)) continue;
@@ -1867,8 +1887,10 @@ __device__ __forceinline__ void solve_station(const fd_station_dev &sd, int dag_
         sh.gfaces = 0;
     }
     csync(sh, 6);
+    if ((tid & 31) < 6) ws.cnt[tid & 31] = 0ull;
+    __syncwarp();
     Counters cn;
-    for (int k = 0; k < 5; k++) cn.n[k] = 0;
+    cn.n = ws.cnt;
     const int nx = sd.g.nx, ny = sd.g.ny, nz = sd.g.nz;
     int guard_sweeps = 0;
     while (sh.reverse > -1 && sh.stat == 0) {
@@ -1935,7 +1957,8 @@ __device__ __forceinline__ void solve_station(const fd_station_dev &sd, int dag_
         if (++guard_sweeps > 1000000) { if (tid == 0 && rank == 0) sh.w->status = 4; break; }
     }
     /* statistics */
-    for (int k = 0; k < 5; k++) atomicAdd(&sh.w->st[k], cn.n[k]);
+    __syncwarp();
+    if ((tid & 31) < 5) atomicAdd(&sh.w->st[tid & 31], ws.cnt[tid & 31]);
     csync(sh, 9);
     if (tid == 0 && rank == 0 && sd.stats) {
         fd_station_stats *o = sd.stats;
