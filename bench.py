@@ -48,11 +48,14 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--stations", type=int, default=None, help="stations per GPU (default 64; config 1: 1)")
     ap.add_argument("--rate", type=float, default=12.0, help="--config 4: request arrivals per second")
-    ap.add_argument("--config", type=int, default=3, choices=[1, 2, 3, 4],
+    ap.add_argument("--config", type=int, default=3, choices=[1, 2, 3, 4, 5],
                     help="3 (default): the 500-window uneven batch, with the config-2 legs; 2: 64 stations of "
                          "201x201x81; 1: the one-station 61x61x31 case, for profiling; 4: served P/S requests; "
                          "5: stations on the full 401x401x161 grid with memory admission (each its own JSON line)")
     ap.add_argument("--no-config2", action="store_true", help="--config 3: leave out the config-2 legs")
+    ap.add_argument("--field-budget", type=int, default=64,
+                    help="--config 5: fields kept on the device (beyond it they spill to pinned host memory)")
+    ap.add_argument("--session-gb", type=int, default=120, help="--config 5: the serving session's device memory")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--serve-requests", type=int, default=300,
                     help="requests of the serving leg (0: skip it)")
@@ -65,7 +68,7 @@ def parse():
                     help="only run a small fixed case of the c2f and location kernels (for ncu captures)")
     args = ap.parse_args()
     if args.stations is None:
-        args.stations = STATIONS_PER_GPU if args.config == 2 else 1
+        args.stations = STATIONS_PER_GPU if args.config == 2 else 152 if args.config == 5 else 1
     return args
 
 
@@ -896,6 +899,83 @@ def run_reference_config3(args):
     shutil.rmtree(case_dir, ignore_errors=True)
 
 
+def run_config5(args):
+    """--config 5: stations on the full 401x401x161 grid with a dipping fast slab (1200 stations, seed
+    5; args.stations of them, the pinned sample first), served by a serving session whose fields stay
+    on the device up to a budget (args.field_budget fields) and are spilled to pinned host memory
+    beyond it (fdtomoc_gb300.fieldstore).  Against the plain form (one station per launch) and, for the
+    pinned sample, against the reference binary's fields.  Prints one JSON line."""
+    import numpy as np
+    import torch
+    from fdtomoc_gb300 import build, lib, workloads as W
+    from fdtomoc_gb300.fieldstore import FieldStore
+    fix = headline_fixture()
+    g, v, sts = W.config(5)
+    pinned = sorted(fix["config5"]) if fix and "config5" in fix else []
+    names = pinned + [s["name"] for s in sts if s["name"] not in pinned]
+    names = names[:max(1, args.stations)]
+    by = {s["name"]: s for s in sts}
+    case_dir = tempfile.mkdtemp(prefix="fdbench_c5_")
+    W.write_case(case_dir, g, v, [by[n] for n in names])
+    build.build()
+    stations = [lib.station_from_par("par=" + os.path.join(case_dir, n + ".par"))[0] for n in names]
+    field_bytes = 4 * g.nx * g.ny * g.nz
+    with lib.Server(0, hbm_bytes=args.session_gb << 30) as sv:
+        sv.set_model(0, v)
+        store = FieldStore(sv, args.field_budget * field_bytes)
+        t0 = time.time()
+        for n, st in zip(names, stations):
+            store.submit(n, st, 0)
+            store.poll(64, 0)
+        store.drain(3600000)
+        wall = time.time() - t0
+        m = sv.metrics()
+        failed = sum(r["status"] != 0 for r in store.results.values())
+        resident = sum(store.where(n) == "device" for n in names)
+        same = None
+        if pinned:
+            ok = 0
+            for n in pinned:
+                f = store.get(n)
+                ok += hashlib_bytes((f.cpu() if f.is_cuda else f).numpy().tobytes()) == fix["config5"][n]["data_sha256"]
+            same = f"{ok}/{len(pinned)}"
+        spilled, direct = store.spilled, store.direct_to_host
+        del store
+    # plain form: one station per launch
+    with lib.Context(0) as ctx:
+        vel = torch.from_numpy(v.reshape(-1)).cuda()
+        slow = torch.empty_like(vel)
+        ctx.velocity_to_slowness(vel.data_ptr(), slow.data_ptr(), v.size)
+        out = torch.empty(stations[0].shape, dtype=torch.float32, device="cuda")
+        torch.cuda.synchronize()
+        tp = time.time()
+        (ps,) = ctx.solve_device(stations[:1], slow.data_ptr(), g.nx, g.nx * g.ny, [out.data_ptr()])
+        plain_s = time.time() - tp
+    value = len(names) / wall
+    line = {
+        "metric": "station fields/s served on the full 401x401x161 grid, fields device-resident up to a budget "
+                  "then spilled to pinned host memory, bit-identical to reference",
+        "value": value, "unit": UNIT, "n_gpus": 1, "steps": 1, "warmup": 0, "ms_per_step": wall * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64 stencils / f32 fields",
+        "data": "synthetic (seeded, config 5 recipe)",
+        "config": {"workload": f"{len(names)} of the 1200 stations on 401x401x161 with a 30-degree dipping +8 % slab "
+                               "(config 5)", "field_budget_fields": args.field_budget,
+                   "session_hbm_gb": args.session_gb},
+        "fields": {"device_resident": resident, "spilled_to_host": spilled, "solved_into_host": direct,
+                   "bytes_each": field_bytes},
+        "latency_ms": {"p50": m["p50_ms"], "p99": m["p99_ms"], "max": m["max_ms"]},
+        "solve_ms": {"p50": m["solve_p50_ms"], "p99": m["solve_p99_ms"]},
+        "node_updates_per_s": m["node_updates"] / wall, "failed": failed, "hbm_peak_bytes": m["hbm_peak"],
+        "plain": {"s_per_station": plain_s, "fields_per_s": 1.0 / plain_s, "served_over_plain": value * plain_s},
+        "parity": {"pinned_stations_bit_identical_to_reference": same,
+                   "against": "SHA-256 of the reference binary's time files for a seeded sample"},
+        "gpu_launches": m["grid_launches"] + 1,
+    }
+    print(json.dumps(line), flush=True)
+    shutil.rmtree(case_dir, ignore_errors=True)
+
+
+
 def run_config4(args):
     """--config 4: served P and S solves.  Requests (station window, phase) drawn from 800 windows
     (61..301 x 61..301 x 61..121 over the 401x401x161 model, seed 4) arrive as a seeded Poisson stream
@@ -1225,6 +1305,8 @@ def main():
         run_config3(args)
     elif args.config == 4 and args.impl != "reference":
         run_config4(args)
+    elif args.config == 5 and args.impl != "reference":
+        run_config5(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

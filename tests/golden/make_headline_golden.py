@@ -1,6 +1,7 @@
 """Pin the benchmark workloads against the reference binary: every station of the 64-station
 201x201x81 workload (config 2) and every one of the 500 uneven windows over the 401x401x161 model
-(config 3).
+(config 3); with --config5, a seeded sample of 8 of the 1200 stations on the full 401x401x161 grid
+with the dipping slab (config 5).
 
 Run where the reference sources are present (oracle/Makefile builds the reference's own sphfd from
 them into oracle/_ref/sphfd_ref; the source root is taken from $FDTOMOC_REFERENCE):
@@ -110,10 +111,81 @@ def sweeps_of(log):
     return 1 + log.count("RESTART at") - log.count("RESTART CANCELLED")
 
 
+CONFIG5_SAMPLE = 8   # config-5 stations pinned (a seeded sample of the 1200: full-grid solves are long)
+
+
+def config5_sample():
+    """The seeded sample of config-5 stations that is pinned: their indices among the 1200."""
+    import numpy as np
+    return sorted(int(k) for k in np.random.default_rng(55).choice(1200, CONFIG5_SAMPLE, replace=False))
+
+
+def main_config5(jobs):
+    """Add the config-5 sample (401x401x161 with the dipping slab) to headline_reference.json."""
+    import numpy as np
+    from fdtomoc_gb300 import workloads as W
+    from fdtomoc_gb300.formats import write_grid, write_par
+    out = json.load(open(OUT))
+    tmp = tempfile.mkdtemp(prefix="headline5_")
+    g, v, sts = W.config(5)
+    vf = os.path.join(tmp, "vp.mod")
+    write_grid(vf, W.head_for(g), v)
+    picks = config5_sample()
+    running, res = [], {}
+    pending = []
+    for k in picks:
+        st = sts[k]
+        pf = os.path.join(tmp, st["name"] + ".par")
+        write_par(pf, W.par_for(g, st, vf, st["name"] + ".ptimes"))
+        pending += [(st["name"], "ref", pf), (st["name"], "oracle", pf)]
+    t_start = time.time()
+    while pending or running:
+        while pending and len(running) < jobs:
+            name, kind, pf = pending.pop(0)
+            outdir = os.path.join(tmp, f"{name}_{kind}")
+            exe = REF_BIN if kind == "ref" else ORACLE_BIN
+            running.append((name, kind, launch(exe, pf, outdir, None if kind == "ref" else {"FDO_MODE": "fast"}),
+                            outdir, time.time()))
+        time.sleep(0.2)
+        still = []
+        for name, kind, p, outdir, t0 in running:
+            if p.poll() is None:
+                still.append((name, kind, p, outdir, t0))
+                continue
+            log = p.stderr.read()
+            if p.returncode != 0:
+                raise RuntimeError(f"{kind} failed on {name}: {log[-2000:]}")
+            b = open(os.path.join(outdir, name + ".ptimes"), "rb").read()
+            shutil.rmtree(outdir)
+            res.setdefault(name, {})[kind] = (b, log, time.time() - t0)
+            print(f"[{time.time() - t_start:7.0f} s] config5/{name} {kind} done", flush=True)
+        running = still
+    out["models"]["config5"] = model_sha(v)
+    out["config5"] = {}
+    for name, h in res.items():
+        rb, rlog, rt = h["ref"]
+        ob, olog, ot = h["oracle"]
+        nu = 0
+        for tok in olog.split():
+            if tok.startswith("node_updates="):
+                nu = int(tok.split("=")[1])
+        out["config5"][name] = {"data_sha256": sha(rb[232:]), "file_sha256": sha(rb), "sweeps": sweeps_of(rlog),
+                                "node_updates": nu, "oracle_equal": rb == ob, "ref_s": round(rt, 2),
+                                "oracle_s": round(ot, 2)}
+    json.dump(out, open(OUT, "w"), indent=0, sort_keys=True)
+    shutil.rmtree(tmp, ignore_errors=True)
+    print(json.dumps({k: (v["sweeps"], v["oracle_equal"]) for k, v in out["config5"].items()}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--jobs", type=int, default=os.cpu_count() or 1)
+    ap.add_argument("--config5", action="store_true",
+                    help="add the pinned sample of config-5 stations to an existing headline_reference.json")
     args = ap.parse_args()
+    if args.config5:
+        subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref", "sphfd_oracle"], check=True)
+        return main_config5(args.jobs)
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref", "sphfd_oracle"], check=True)
     assert os.path.exists(REF_BIN), "reference binary not built (are the reference sources present?)"
     tmp = tempfile.mkdtemp(prefix="headline_")
