@@ -53,7 +53,7 @@ def parse():
                          "201x201x81; 1: the one-station 61x61x31 case, for profiling; 4: served P/S requests; "
                          "5: stations on the full 401x401x161 grid with memory admission (each its own JSON line)")
     ap.add_argument("--no-config2", action="store_true", help="--config 3: leave out the config-2 legs")
-    ap.add_argument("--field-budget", type=int, default=64,
+    ap.add_argument("--field-budget", type=int, default=6,
                     help="--config 5: fields kept on the device (beyond it they spill to pinned host memory)")
     ap.add_argument("--session-gb", type=int, default=120, help="--config 5: the serving session's device memory")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -68,7 +68,7 @@ def parse():
                     help="only run a small fixed case of the c2f and location kernels (for ncu captures)")
     args = ap.parse_args()
     if args.stations is None:
-        args.stations = STATIONS_PER_GPU if args.config == 2 else 152 if args.config == 5 else 1
+        args.stations = STATIONS_PER_GPU if args.config == 2 else 16 if args.config == 5 else 1
     return args
 
 
@@ -946,11 +946,14 @@ def run_config5(args):
         vel = torch.from_numpy(v.reshape(-1)).cuda()
         slow = torch.empty_like(vel)
         ctx.velocity_to_slowness(vel.data_ptr(), slow.data_ptr(), v.size)
-        out = torch.empty(stations[0].shape, dtype=torch.float32, device="cuda")
+        # the pinned station with the fewest sweeps (full-grid solves with many restarts take minutes)
+        kp = min(range(len(pinned)), key=lambda k: fix["config5"][pinned[k]]["sweeps"]) if pinned else 0
+        out = torch.empty(stations[kp].shape, dtype=torch.float32, device="cuda")
         torch.cuda.synchronize()
         tp = time.time()
-        (ps,) = ctx.solve_device(stations[:1], slow.data_ptr(), g.nx, g.nx * g.ny, [out.data_ptr()])
+        (ps,) = ctx.solve_device([stations[kp]], slow.data_ptr(), g.nx, g.nx * g.ny, [out.data_ptr()])
         plain_s = time.time() - tp
+        plain_nu = ps["node_updates"]
     value = len(names) / wall
     line = {
         "metric": "station fields/s served on the full 401x401x161 grid, fields device-resident up to a budget "
@@ -966,7 +969,10 @@ def run_config5(args):
         "latency_ms": {"p50": m["p50_ms"], "p99": m["p99_ms"], "max": m["max_ms"]},
         "solve_ms": {"p50": m["solve_p50_ms"], "p99": m["solve_p99_ms"]},
         "node_updates_per_s": m["node_updates"] / wall, "failed": failed, "hbm_peak_bytes": m["hbm_peak"],
-        "plain": {"s_per_station": plain_s, "fields_per_s": 1.0 / plain_s, "served_over_plain": value * plain_s},
+        "plain": {"station": names[kp], "s_per_station": plain_s, "node_updates": plain_nu,
+                  "node_updates_per_s": plain_nu / plain_s,
+                  "served_node_updates_over_plain": (m["node_updates"] / wall) / (plain_nu / plain_s),
+                  "note": "stations here differ by up to 4x in sweeps, so node updates/s compare the forms"},
         "parity": {"pinned_stations_bit_identical_to_reference": same,
                    "against": "SHA-256 of the reference binary's time files for a seeded sample"},
         "gpu_launches": m["grid_launches"] + 1,
