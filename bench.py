@@ -72,6 +72,13 @@ def parse():
     return args
 
 
+def under_profiler() -> bool:
+    """Whether a CUDA profiler (Nsight Compute) is injected into this process: it sets one of these
+    variables (which one depends on the tool's version)."""
+    return any(os.environ.get(k) for k in ("CUDA_INJECTION64_PATH", "NV_NSIGHT_INJECTION_TRANSPORT_TYPE",
+                                            "NV_TPS_LAUNCH_TOKEN", "NVIDIA_PROCESS_INJECTION_XML_TARGET_SETTINGS"))
+
+
 def dist_env():
     return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
             int(os.environ.get("LOCAL_RANK", 0)))
@@ -853,7 +860,7 @@ def config2_legs(args, lib, ctx, stream, fix):
         out["c2f"] = c2f_leg(args, lib, ctx, stream)
     if args.ray_events > 0:
         out["rays"] = ray_leg(args, lib, ctx, g, sts, fields, stream)
-    profiled = bool(os.environ.get("CUDA_INJECTION64_PATH"))
+    profiled = under_profiler()
     if args.serve_requests > 0 and not profiled:
         out["serving"] = serve_leg(args, lib, stations, v, fields)
     shutil.rmtree(case_dir, ignore_errors=True)
@@ -1199,7 +1206,7 @@ def run_gpu(args):
     # the serving session's long-running grid waits on its host thread; under a profiler that
     # serialises launches the launching call would not return while the grid waits, so the leg is
     # left out there
-    profiled = bool(os.environ.get("CUDA_INJECTION64_PATH"))
+    profiled = under_profiler()
     serving = serve_leg(args, lib, stations, v, fields) if args.serve_requests > 0 and not profiled else None
 
     # roofline of the solve kernel (one launch per step): algorithmic bytes 12 B per node update
