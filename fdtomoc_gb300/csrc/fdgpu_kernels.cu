@@ -1409,6 +1409,7 @@ __device__ void run_walk(const fd_station_dev &sd, Shared &sh, const CtaSmem &cs
     const long long wait_lim = sd.wait_cycles > 0 ? sd.wait_cycles : FD_WAIT_CYCLES;
     const long long walk_lim = sd.walk_cycles > 0 ? sd.walk_cycles : FD_WALK_CYCLES;
     long long chunks = 0;
+    unsigned idle_polls = 0;
     for (;;) {
         int act = 0, h = 0, m = 0, qf = 0;   /* act: 0 wait, 1 chunk, 2 resume a waiter, 3 leave */
         if (lane == 0) {
@@ -1435,9 +1436,12 @@ __device__ void run_walk(const fd_station_dev &sd, Shared &sh, const CtaSmem &cs
                             act = 1; h = sh.w->qbase[best] + bhead; m = want; qf = best;
                         }
                     } else {
-                        if (!idle) { wfence(sh); atomicAdd(&sh.w->idle, 1); idle = true; }
-                        /* all idle with nothing queued and nodes left: nothing can release them */
-                        if (quiescent(sh) && vload(sh.w->ndone) < total) {
+                        if (!idle) { wfence(sh); atomicAdd(&sh.w->idle, 1); idle = true; idle_polls = 0; }
+                        /* all idle with nothing queued and nodes left: nothing can release them.  The
+                         * check (two fences and a scan of every queue) runs on every 64th idle poll
+                         * only: idle warps are most of the CTA in a forward sweep, and their polls
+                         * share the SM's shared-memory pipe with the working warps */
+                        if ((++idle_polls & 63u) == 0u && quiescent(sh) && vload(sh.w->ndone) < total) {
                             atomicCAS(&sh.w->status, 0, 3);
                             act = 3;
                         }
