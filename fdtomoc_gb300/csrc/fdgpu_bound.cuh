@@ -152,7 +152,7 @@ __device__ __forceinline__ float lower_2d(const TrialDesc &d, const float *t18, 
 /* trial value v (>= the returned bound lo) cannot lower a running minimum that is at most g */
 __device__ __forceinline__ bool bound_prunes(float lo, double g)
 {
-    return lo >= 0.f && g <= 1.e11 && !lt(f2d(lo), g);
+    return lo >= 0.f && !lt(1.e11, g) && !lt(f2d(lo), g);
 }
 
 }  // namespace fdk

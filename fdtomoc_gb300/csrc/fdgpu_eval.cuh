@@ -50,6 +50,27 @@ __device__ __forceinline__ double f2d(float f)
     return (double)f;
 }
 
+/* Comparisons of finite doubles on the integer pipe (an FP64 compare occupies this GPU's FP64 unit
+ * like any FP64 instruction, 64 cycles per warp).  Each gives exactly the double comparison's result,
+ * signed zeros included, for the operands it states; none is used where an operand may be NaN. */
+
+/* a < b for finite a and b of any sign */
+__device__ __forceinline__ bool flt(double a, double b)
+{
+    const long long ia = __double_as_longlong(a), ib = __double_as_longlong(b);
+    if ((ia | ib) >= 0) return ia < ib;                       /* both non-negative */
+    if ((ia & ib) < 0) return ia > ib;                        /* both negative: the larger magnitude */
+    if (ia < 0) return (ia << 1) != 0 || (ib << 1) != 0;      /* a negative: below b unless both zero */
+    return false;                                             /* b negative, a not */
+}
+
+/* !(x >= 0.) for any x: negative and not -0, or NaN */
+__device__ __forceinline__ bool not_ge0(double x)
+{
+    const long long ix = __double_as_longlong(x);
+    return (ix < 0 && (ix << 1) != 0) || (ix & 0x7fffffffffffffffll) > 0x7ff0000000000000ll;
+}
+
 /* x * 2^k, exact: exponent arithmetic on the integer pipe when x and the result are normal;
  * zeros and subnormals take the floating-point multiply (never reached with physical inputs) */
 template <int K>
@@ -119,27 +140,27 @@ __host__ __device__ constexpr int chain_class(fdn_chain c)
  * causality test against floor tmx; tie rule of fdsph3d (x1 preferred only if strictly smaller). */
 __device__ __forceinline__ double roots_3d(double b, double rad, double twoa, double i2a, double tmx)
 {
-    if (!(rad >= 0.)) return 1.e11;
+    if (not_ge0(rad)) return 1.e11;
     const double sq = __dsqrt_rn(rad);
     const double x1 = div_rn(-b + sq, twoa, i2a);
     const double x2 = div_rn(-b - sq, twoa, i2a);
-    const bool bad1 = x1 < tmx, bad2 = x2 < tmx;
+    const bool bad1 = flt(x1, tmx), bad2 = flt(x2, tmx);
     if (bad1) return bad2 ? 1.e11 : x2;
     if (bad2) return x1;
-    return (x1 < x2) ? x1 : x2;
+    return flt(x1, x2) ? x1 : x2;
 }
 
 /* same, with the tie rule of fdsphne / fdsph2d (x2 preferred only if strictly smaller) */
 __device__ __forceinline__ double roots_2(double b, double rad, double twoa, double i2a, double tmx)
 {
-    if (!(rad >= 0.)) return 1.e11;
+    if (not_ge0(rad)) return 1.e11;
     const double sq = __dsqrt_rn(rad);
     const double x1 = div_rn(-b + sq, twoa, i2a);
     const double x2 = div_rn(-b - sq, twoa, i2a);
-    const bool bad1 = x1 < tmx, bad2 = x2 < tmx;
+    const bool bad1 = flt(x1, tmx), bad2 = flt(x2, tmx);
     if (bad1) return bad2 ? 1.e11 : x2;
     if (bad2) return x1;
-    return (x2 < x1) ? x2 : x1;
+    return flt(x2, x1) ? x2 : x1;
 }
 
 }  // namespace fdk

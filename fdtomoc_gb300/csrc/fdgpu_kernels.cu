@@ -417,7 +417,7 @@ __device__ __forceinline__ float floor_of(const float *t18)
 /* a trial with floor fl cannot lower a running minimum that is at most g (any earlier value of
  * the running minimum is such a bound): its accepted value is >= fl, and its rejection value
  * 1e11 is not below g */
-__device__ __forceinline__ bool prunable(float fl, double g) { return f2d(fl) >= g && g <= 1.e11; }
+__device__ __forceinline__ bool prunable(float fl, double g) { return !lt(f2d(fl), g) && !lt(1.e11, g); }
 
 struct Rect {
     int u, v, nu, nv, ulo, uhi, vlo, vhi;
@@ -446,9 +446,9 @@ __device__ __forceinline__ void guard_trials(const float *t18, const Rect &r, do
             if constexpr (tr.kind == FDN_3D) {
                 if (!prunable(floor_of<F, K>(t18), g0)) em |= 1u << K;
             } else if constexpr (tr.kind == FDN_1D) {
-                if (!(f2d(floor_of<F, K>(t18)) >= g0)) em |= 1u << K;
+                if (lt(f2d(floor_of<F, K>(t18)), g0)) em |= 1u << K;
             } else if constexpr (tr.kind == FDN_NE) {
-                if (!any3d && g0 > 1.0e9 && !prunable(floor_of<F, K>(t18), g0)) em |= 1u << K;
+                if (!any3d && lt(1.0e9, g0) && !prunable(floor_of<F, K>(t18), g0)) em |= 1u << K;
             }
         }
         guard_trials<F, K + 1>(t18, r, g0, any3d, gm, em);
@@ -508,14 +508,14 @@ __device__ void eval_items(const fd_station_dev &sd, const TrialDesc *dsc, WarpS
         case 2: {
             double x1, x2;
             eval_2d(d, t18, s18, sd.g, z, y, x1, x2);
-            if (x1 != x1) {
+            if ((__double_as_longlong(x1) & 0x7fffffffffffffffll) > 0x7ff0000000000000ll) {   /* NaN: no root */
                 v = 1.e11;
             } else {
                 const float fl = fmaxf(fmaxf(fmaxf(t18[d.slot[1]], t18[d.slot[2]]), fmaxf(t18[d.slot[3]], ws.s0[slot])),
                                        ws.s4[slot]);
                 const double f = f2d(fl);
-                const bool bad1 = lt(x1, f), bad2 = lt(x2, f);
-                v = bad1 ? (bad2 ? 1.e11 : x2) : (bad2 ? x1 : (lt(x2, x1) ? x2 : x1));
+                const bool bad1 = flt(x1, f), bad2 = flt(x2, f);
+                v = bad1 ? (bad2 ? 1.e11 : x2) : (bad2 ? x1 : (flt(x2, x1) ? x2 : x1));
             }
             break;
         }
@@ -1159,7 +1159,7 @@ __device__ void warp_chunk(const fd_station_dev &sd, Shared &sh, const CtaSmem &
         guards(F, tr, wh.r, gm, em);
         /* a 2-D trial before any corner / new-edge call reads the state an earlier point left */
         const double told = f2d(tr[NB_POINT]);
-        permissive = !have_inherit && (gm & 0xFu) == 0 && !((gm & 0xF0u) && told > 1.0e9) && (gm & 0xFF00u);
+        permissive = !have_inherit && (gm & 0xFu) == 0 && !((gm & 0xF0u) && lt(1.0e9, told)) && (gm & 0xFF00u);
     }
     __syncwarp();
     int n1 = push_items(ws.items, 0, em, TK_3D0, TK_2D0, lane);

@@ -267,7 +267,7 @@ __device__ __forceinline__ void eval_2d(const TrialDesc &d, const float *t18, co
     const double b = scale2k<1>(div_rn(t1t3t2, dd[1], iv[1]) + div_rn(t2t3t1, dd[0], iv[0]));
     const double c = (t1t3t2 * t1t3t2 + t2t3t1 * t2t3t1) - sum * slo;
     const double rad = b * b - scale2k<2>(a) * c;
-    if (!(rad >= 0.)) {
+    if (not_ge0(rad)) {
         x1 = __longlong_as_double(0x7ff8000000000000ll);
         x2 = x1;
         return;
@@ -293,9 +293,9 @@ __device__ __forceinline__ double eval_nf(const TrialDesc &d, const float *t18, 
     const double t4t0 = div_rn(f2d(tf[4]) - f2d(tf[0]), dd[0], iv[0]);
     const double t1t3 = div_rn(f2d(tf[1]) - f2d(tf[3]), dd[1], iv[1]);
     double x = slo * slo - scale2k<-2>(t4t0 * t4t0 + t1t3 * t1t3);
-    if (!(x >= 0.)) return 1.e11;
+    if (not_ge0(x)) return 1.e11;
     x = f2d(tf[2]) + dd[2] * __dsqrt_rn(x);
-    return (x < f2d(tchk)) ? 1.e11 : x;
+    return flt(x, f2d(tchk)) ? 1.e11 : x;
 }
 
 /* straight edge: t_nbr + 0.5*(s_point + s_nbr) * f1 * f2 * f3 (e.g. src/sphfd.c:1727-1755) */
