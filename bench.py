@@ -749,6 +749,10 @@ def run_config3(args):
     e2e_s = time.time() - t0
     if rc != 0:
         raise RuntimeError(f"fdgpu_solve_host failed: {rc}")
+    if world > 1:
+        t = torch.tensor([e2e_s], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
     e2e_same = None
     if fix:
         e2e_same = sum(hashlib_bytes(o.numpy().tobytes()) == fix["config3"][w["name"]]["data_sha256"]
