@@ -35,3 +35,24 @@ def test_parlist_and_spec(tmp_path):
     spec = parfiles.write_parlist(["/a/x.par", "/a/x.spar"], str(tmp_path / "pl"), "/t", str(tmp_path / "spec"))
     assert (tmp_path / "pl").read_text() == "par=/a/x.par\npar=/a/x.spar\n"
     assert open(spec).read() == f"parlist {tmp_path / 'pl'}\ntimedir /t\n"
+
+
+def test_driver_reads_spec_and_parlist(tmp_path):
+    """sphfd's main reads "parlist" and "timedir" from its spec, then every "par=" line (at most
+    MAXNUMPAR = 2000, src/sphfd.c:143); the rank-aware driver does the same."""
+    import pytest
+    from fdtomoc_gb300 import driver
+    (tmp_path / "pl").write_text("par=/a/x.par\n\npar=/a/y.spar\n")
+    (tmp_path / "spec").write_text(f"timedir /t/out\nother 1\nparlist {tmp_path / 'pl'}\n")
+    assert driver.read_spec(str(tmp_path / "spec")) == (str(tmp_path / "pl"), "/t/out")
+    assert driver.read_parlist(str(tmp_path / "pl")) == ["par=/a/x.par", "par=/a/y.spar"]
+    (tmp_path / "big").write_text("".join(f"par=/a/{k}.par\n" for k in range(driver.MAXNUMPAR + 1)))
+    with pytest.raises(ValueError):
+        driver.read_parlist(str(tmp_path / "big"))
+    (tmp_path / "bad").write_text("parlist x\n")
+    with pytest.raises(ValueError):
+        driver.read_spec(str(tmp_path / "bad"))
+    # without torch.distributed the driver is the plain parlist call
+    seen = []
+    st = driver.run_entries(["par=/a/x.par"], str(tmp_path / "o"), lambda e, d: seen.append((e, d)) or [0])
+    assert st == [0] and seen == [(["par=/a/x.par"], str(tmp_path / "o"))]
