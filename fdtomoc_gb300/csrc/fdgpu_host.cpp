@@ -396,6 +396,15 @@ int prepare_batch(fdgpu_ctx *ctx, int n, const fdgpu_station *st, const float *s
     return FDGPU_OK;
 }
 
+/* a station's measured solve time into the context's table: the mean of the last value and the new one,
+ * so that one run's noise (a solve's time depends on what runs beside it) moves the order less */
+void record_time(fdgpu_ctx *ctx, const fdgpu_station &s, long long ns)
+{
+    auto it = ctx->solve_ns.find(station_key(s));
+    if (it == ctx->solve_ns.end()) ctx->solve_ns[station_key(s)] = ns;
+    else it->second = (it->second + ns) / 2;
+}
+
 /* The public statistics of n solves from their device records (queued on cs, then waited for).
  * Clean solves' times go into the context's launch-order table (st: the stations, in the caller's
  * order). */
@@ -410,7 +419,7 @@ int read_stats(fdgpu_ctx *ctx, const DevBuf &stats_buf, int n, fdgpu_stats *stat
         if (stats) fdh::copy_stats(stats[k], hst[k]);
         if (hst[k].status && rc == FDGPU_OK) rc = FDGPU_ESCHED;
         if (st && !hst[k].status && hst[k].t_end_ns > hst[k].t_start_ns)
-            ctx->solve_ns[station_key(st[k])] = hst[k].t_end_ns - hst[k].t_start_ns;
+            record_time(ctx, st[k], hst[k].t_end_ns - hst[k].t_start_ns);
     }
     return rc;
 }
@@ -545,20 +554,24 @@ extern "C" int fdgpu_batch_tune_order(fdgpu_batch *b, void *stream)
     if (!b) return FDGPU_EINVAL;
     fdgpu_ctx *ctx = b->ctx;
     cudaStream_t cs = stream ? (cudaStream_t)stream : ctx->stream;
-    std::vector<fd_station_dev> rec;
-    std::vector<int> idx;
-    int rc = batch_records(b, rec, idx, cs);
-    if (rc) return rc;
     std::vector<fd_station_stats> hst(b->n);
     FD_CU(ctx, cudaMemcpyAsync(hst.data(), b->bufs.stats.p, sizeof(fd_station_stats) * b->n, cudaMemcpyDeviceToHost, cs));
     FD_CU(ctx, cudaStreamSynchronize(cs));
     for (int k = 0; k < b->n; k++)
         if (hst[k].t_end_ns <= hst[k].t_start_ns || hst[k].status) return FDGPU_EINVAL;   /* no clean run yet */
-    /* longest measured solve first; equal times keep the current order */
+    /* the last run's times into the context's table (blended with earlier ones), then longest first
+     * by the table; equal times keep the current order */
+    std::vector<long long> t(b->n);
+    for (int k = 0; k < b->n; k++) {
+        record_time(ctx, b->stations[k], hst[k].t_end_ns - hst[k].t_start_ns);
+        t[k] = ctx->solve_ns[station_key(b->stations[k])];
+    }
+    std::vector<fd_station_dev> rec;
+    std::vector<int> idx;
+    int rc = batch_records(b, rec, idx, cs);
+    if (rc) return rc;
     std::vector<int> order(idx);
-    std::stable_sort(order.begin(), order.end(), [&](int a, int c) {
-        return hst[a].t_end_ns - hst[a].t_start_ns > hst[c].t_end_ns - hst[c].t_start_ns;
-    });
+    std::stable_sort(order.begin(), order.end(), [&](int a, int c) { return t[a] > t[c]; });
     return fdgpu_batch_set_order(b, order.data(), stream);
 }
 

@@ -151,17 +151,19 @@ void fdgpu_batch_destroy(fdgpu_batch *batch);
 /* Launch order of a prepared batch (no counterpart in the reference, whose OpenMP loop takes par
  * files in list order).  CTA k solves the k-th station of the order, and CTAs beyond the resident
  * ones start as earlier ones finish, so the batch ends sooner when its longest solves start first.
- * A new batch is ordered by grid size; fdgpu_batch_tune_order reorders it by the solve times its
- * last run measured, longest first (an inversion loop re-solves the same stations every
- * iteration, so one run's times predict the next run's).  fdgpu_batch_order reads the order (the
+ * A new batch is ordered by grid size (or by the context's measured times, see below);
+ * fdgpu_batch_tune_order reorders it longest first by the solve times its last run measured, each
+ * blended with the context's earlier measurement of that station (the mean of the two), so that
+ * one run's noise moves the order less (an inversion loop re-solves the same stations every
+ * iteration, so earlier runs' times predict the next run's).  fdgpu_batch_order reads the order (the
  * caller's station indices, in launch order) and fdgpu_batch_set_order sets one, e.g. saved from an
  * earlier process.  These copy on `stream` and wait for it: call them between runs, not while one
  * is in flight.  The order changes which CTA solves which station, never a result. */
 int fdgpu_batch_order(fdgpu_batch *batch, int *order, void *stream);
 
 /* The context's launch-order table: every clean solve of fdgpu_solve_device / fdgpu_solve_host /
- * fdgpu_batch_stats records each station's measured solve time, and a later batch whose stations all
- * have one is launched longest first (otherwise largest grid first).  order_save writes the table to
+ * fdgpu_batch_stats records each station's measured solve time (the mean of the new time and the
+ * one recorded before), and a later batch whose stations all have one is launched longest first (otherwise largest grid first).  order_save writes the table to
  * a file and order_load merges one into the context, so that a new process (the next inversion
  * iteration, say) starts with the order the last one measured.  Results never depend on it.  No
  * counterpart in the reference. */
