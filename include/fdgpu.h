@@ -163,10 +163,10 @@ int fdgpu_batch_order(fdgpu_batch *batch, int *order, void *stream);
 
 /* The context's launch-order table: every clean solve of fdgpu_solve_device / fdgpu_solve_host /
  * fdgpu_batch_stats records each station's measured solve time (the mean of the new time and the
- * one recorded before), and a later batch whose stations all have one is launched longest first (otherwise largest grid first).  order_save writes the table to
- * a file and order_load merges one into the context, so that a new process (the next inversion
- * iteration, say) starts with the order the last one measured.  Results never depend on it.  No
- * counterpart in the reference. */
+ * one recorded before), and a later batch whose stations all have one is launched longest first
+ * (otherwise largest grid first).  order_save writes the table to a file and order_load merges one
+ * into the context, so that a new process (the next inversion iteration, say) starts with the
+ * order the last one measured.  Results never depend on it.  No counterpart in the reference. */
 int fdgpu_order_save(const fdgpu_ctx *ctx, const char *path);
 int fdgpu_order_load(fdgpu_ctx *ctx, const char *path);
 int fdgpu_batch_set_order(fdgpu_batch *batch, const int *order, void *stream);
