@@ -32,6 +32,7 @@ class FieldStore:
         self.pending = {}                  # request id -> key
         self.resident = collections.OrderedDict()   # finished device-resident keys, oldest first
         self.copies = []                   # (event, device tensor) of spills not yet known complete
+        self.spill_event = {}              # key -> the event of its spill copy
         self.stream = torch.cuda.Stream(device)
         self.results = {}                  # key -> the request's result
         self.spilled = 0
@@ -62,6 +63,7 @@ class FieldStore:
             ev.record(self.stream)
         t.record_stream(self.stream)
         self.copies.append((ev, t))
+        self.spill_event[key] = ev
         self.host[key] = h
         self.used -= t.numel() * 4
         self.spilled += 1
@@ -72,15 +74,18 @@ class FieldStore:
         need = self._bytes(station)
         while self.used + need > self.budget and self.resident:
             self._spill(next(iter(self.resident)))
-        if self.used + need <= self.budget:
+        on_device = self.used + need <= self.budget
+        if on_device:
             out = torch.empty(station.shape, dtype=torch.float32, device=f"cuda:{self.device}")
+        else:
+            out = torch.empty(station.shape, dtype=torch.float32, pin_memory=True)
+        rid = self.sv.submit(station, model, out, init=init, tag=tag)   # raises before anything is kept
+        if on_device:
             self.dev[key] = out
             self.used += need
         else:
-            out = torch.empty(station.shape, dtype=torch.float32, pin_memory=True)
             self.host[key] = out
             self.direct_to_host += 1
-        rid = self.sv.submit(station, model, out, init=init, tag=tag)
         self.pending[rid] = key
         return rid
 
@@ -103,7 +108,11 @@ class FieldStore:
         self._reap(wait=True)
 
     def get(self, key):
-        """The field: a device tensor if resident, else a pinned host tensor."""
+        """The field: a device tensor if resident, else a pinned host tensor (once its spill copy, if
+        any, has finished).  Call it after the request's result has been polled."""
+        ev = self.spill_event.pop(key, None)
+        if ev is not None:
+            ev.synchronize()
         return self.dev.get(key, self.host.get(key))
 
     def where(self, key) -> str:
