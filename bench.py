@@ -776,9 +776,14 @@ def run_config3(args):
     peak = peaks.get("hbm_gbs", 6800.0)
     achieved = ALGO_BYTES_PER_NODE_UPDATE * nu / (ms_step / 1e3) / 1e9
     traffic = None
+    traffic_note = None
     tpath = os.path.join(ROOT, "profiles", "fd_solve_traffic.json")
     if os.path.exists(tpath):
-        traffic = json.load(open(tpath))["dram_bytes_per_node_update"] * nu
+        tj = json.load(open(tpath))
+        traffic = tj["dram_bytes_per_node_update"] * nu
+        traffic_note = (f"{tj['dram_bytes_per_node_update']} DRAM B per node update from an ncu capture of "
+                        f"{tj['workload']}, scaled to this launch's node updates; a lower bound here: "
+                        f"{tj['scaling_note']}")
     st_sum = [sum(s_["stencils"][k] for s_ in stats) for k in range(5)]
     fp64_ops = 116 * st_sum[0] + 70 * st_sum[1] + 69 * st_sum[2] + 25 * st_sum[3] + 6 * st_sum[4]
     fp64_peak = ctx.probe_fp64_gops()
@@ -802,7 +807,8 @@ def run_config3(args):
             "e2e": e2e,
             "gpu_launches": args.steps,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "traffic": traffic, "peak_kind": "of measured (MEASURED_PEAKS.json hbm_gbs)",
+                         "traffic": traffic, "traffic_note": traffic_note,
+                         "peak_kind": "of measured (MEASURED_PEAKS.json hbm_gbs)",
                          "note": "the path is bound by FP64 issue and dependency latency, not HBM"},
             "fp64": {"achieved_gops": fp64_ops / (ms_step / 1e3) / 1e9, "peak_gops": fp64_peak,
                      "frac": fp64_ops / (ms_step / 1e3) / 1e9 / fp64_peak,
