@@ -680,11 +680,11 @@ def run_config3(args):
     tuned = False
     for k in range(args.warmup):
         batch.run(stream.cuda_stream)
-        if k <= 1:
-            # longest measured solve first from here on: tuned on the first run (launched largest grid
-            # first), then once more on the first two runs' times averaged, and kept.  Measured over 6
-            # runs on one box: 22.4 s per step, against 23.5 s when tuned once and 22.3 - 25.7 s when
-            # re-tuned after every run
+        if k == 0:
+            # longest measured solve first from here on, tuned on the first run (launched largest grid
+            # first) and kept: over nine runs on several boxes 21.4 - 23.5 s per step; re-tuning after
+            # every run oscillated (22.3 - 25.7 s), tuning twice gave 22.4 s on one box and 25.5 s on
+            # another
             batch.tune_order(stream.cuda_stream)
             tuned = True
     stream.synchronize()
@@ -794,7 +794,7 @@ def run_config3(args):
             "vs_baseline": None, "dtype": "f64 stencils / f32 fields", "data": "synthetic (seeded, config 3 recipe)",
             "config": {"workload": C3_WORKLOAD, "windows_per_gpu": len(wins), "nodes_per_gpu": int(sum(sizes)),
                        "launch": "one prepared batch (fdgpu_batch_run), one kernel per step",
-                       "launch_order": "longest measured solve first (tuned on the first two warm-up runs)" if tuned
+                       "launch_order": "longest measured solve first (tuned on the first warm-up run)" if tuned
                        else "largest grid first",
                        "l2": "inputs larger than L2 (500 fields, 4.7 GB, + 104 MB model)",
                        "parallelism": f"windows x{world}"},
