@@ -139,3 +139,17 @@ def test_batch_equals_alone(gpu_lib, tmp_path):
         for k, (a, b, w) in enumerate(zip(alone, bufs, wins)):
             got = b[1:1 + w.nx * w.ny * w.nz].cpu().numpy()
             assert np.array_equal(a.reshape(-1).view(np.uint32), got.view(np.uint32)), f"window {k} (device)"
+
+
+def test_ps_stations_over_a_device_list(gpu_lib, tmp_path):
+    """fdgpu_sphfd_parlist_devices with device 0 listed twice: two worker threads, each with its own
+    context on the one GPU, share the stations of each velocity file; the files are the reference's."""
+    paths, _, _ = ps_station_case(str(tmp_path / "in"))
+    out = tmp_path / "out"
+    os.makedirs(out)
+    st = gpu_lib.sphfd_parlist(["par=" + p for p in paths], str(out), devices=[0, 0])
+    assert st == [0] * len(paths)
+    got = {f: _sha(out / f) for f in sorted(os.listdir(out))}
+    assert got == GOLD["ps_stations"]
+    with pytest.raises(gpu_lib.FdgpuError):
+        gpu_lib.sphfd_parlist(["par=" + paths[0]], str(out), devices=[0, 4096])
