@@ -15,7 +15,10 @@
  *
  * Set-up: the first call on a device looks up the array's device address with
  * cudaGetSymbolAddress (host code cannot use the array's name as a device pointer) and caches it
- * for that device.  Make that first call before any stream capture on the device.  The cached
+ * for that device.  The call cannot be captured in a CUDA graph: it waits for its solve and copies
+ * the statistics to the host.  Its first call on a device may also load the module, which a stream
+ * capture in global mode elsewhere in the process would reject, so make that first call while no
+ * stream is capturing.  The cached
  * address belongs to the device's primary context: after cudaDeviceReset it is stale, and the
  * entry point must not be called again in that process.
  *

@@ -190,7 +190,8 @@ int fdgpu_probe_fp64(fdgpu_ctx *ctx, double *gops);
  * statistics, geometry tables, face-walk scratch) lives in one static device array of
  * FDGPU_NOALLOC_SCRATCH_BYTES per GPU, held from library load to process exit.  A station that needs
  * more returns FDGPU_ETOOBIG before any GPU work; a 201x201x81 grid needs about 12 MiB.  The first
- * call on a device looks up the array's address; make it before any stream capture.  That address
+ * call on a device looks up the array's address; make it while no stream is capturing.  The call
+ * itself cannot be captured in a CUDA graph (it waits for the solve).  That address
  * is kept for the life of the process: it does not survive cudaDeviceReset (or any other teardown
  * of the device's primary context), after which this entry point must not be called again.  The
  * call runs on the calling thread's current device, and `stream` (a cudaStream_t, NULL = the
