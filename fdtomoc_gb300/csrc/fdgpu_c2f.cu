@@ -24,6 +24,7 @@
 #include <vector>
 
 #include "fdgpu.h"
+#include "fdgpu_device.h"
 
 namespace {
 
@@ -157,7 +158,8 @@ extern "C" int fdgpu_c2f_plan_create(fdgpu_ctx *ctx, const fdgpu_c2f_grid *g, fd
     if (rc) return rc;
     if (!(g->h > 0)) return FDGPU_EINVAL;
     const int dev = fdh_ctx_device(ctx);
-    if (cudaSetDevice(dev) != cudaSuccess) return FDGPU_ENODEV;
+    FdDeviceScope dev_(dev);
+    if (dev_.err) return FDGPU_ENODEV;
     std::vector<Axis> ax, ay, az;
     axis_table(g->nxc, g->igridx, g->x0, g->h, nx, ax);
     axis_table(g->nyc, g->igridy, g->y0, g->h, ny, ay);
@@ -199,6 +201,8 @@ extern "C" int fdgpu_c2f_run(fdgpu_c2f_plan *p, const float *d_coarse, float *d_
 {
     if (!p || !d_coarse || !d_fine) return FDGPU_EINVAL;
     cudaStream_t st = stream ? (cudaStream_t)stream : (cudaStream_t)fdh_ctx_stream(p->ctx);
+    FdDeviceScope dev_(p->device);
+    if (dev_.err) return FDGPU_ENODEV;
     const int nc2 = 2 * p->nxc * p->nyc * p->nzc;
     c2f_slowness<<<(nc2 + 255) / 256 < 1024 ? (nc2 + 255) / 256 : 1024, 256, 0, st>>>(d_coarse, p->slow, nc2);
     const long long rows = 2ll * p->nz * p->ny;
@@ -214,7 +218,7 @@ extern "C" int fdgpu_c2f_run(fdgpu_c2f_plan *p, const float *d_coarse, float *d_
 extern "C" void fdgpu_c2f_plan_destroy(fdgpu_c2f_plan *p)
 {
     if (!p) return;
-    cudaSetDevice(p->device);
+    FdDeviceScope dev_(p->device);
     if (p->mem) {
         cudaDeviceSynchronize();
         cudaFree(p->mem);

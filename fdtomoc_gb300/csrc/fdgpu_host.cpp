@@ -23,6 +23,7 @@
 #include <tuple>
 #include <vector>
 
+#include "fdgpu_device.h"
 #include "fdgpu_layout.h"
 #include "fdgpu_station.h"
 
@@ -175,7 +176,8 @@ extern "C" int fdgpu_create(int device, fdgpu_ctx **out)
     *out = nullptr;
     int n = 0;
     if (cudaGetDeviceCount(&n) != cudaSuccess || n <= device || device < 0) return FDGPU_ENODEV;
-    if (cudaSetDevice(device) != cudaSuccess) return FDGPU_ENODEV;
+    FdDeviceScope dev_(device);
+    if (dev_.err) return FDGPU_ENODEV;
     auto *ctx = new (std::nothrow) fdgpu_ctx;
     if (!ctx) return FDGPU_ENOMEM;
     ctx->device = device;
@@ -190,7 +192,7 @@ extern "C" int fdgpu_create(int device, fdgpu_ctx **out)
 extern "C" void fdgpu_destroy(fdgpu_ctx *ctx)
 {
     if (!ctx) return;
-    cudaSetDevice(ctx->device);
+    FdDeviceScope dev_(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     cudaStream_t s = ctx->stream;
     delete ctx;   /* frees every device buffer it holds */
@@ -219,7 +221,8 @@ extern "C" const char *fdgpu_last_error(const fdgpu_ctx *ctx) { return ctx ? ctx
 extern "C" int fdgpu_probe_fp64(fdgpu_ctx *ctx, double *gops)
 {
     if (!ctx || !gops) return FDGPU_EINVAL;
-    FD_CU(ctx, cudaSetDevice(ctx->device));
+    FdDeviceScope dev_(ctx->device);
+    FD_CU(ctx, dev_.err);
     int sms = 0;
     FD_CU(ctx, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
     const int blocks = sms * 8, threads = 256, iters = 2048;
@@ -243,6 +246,8 @@ extern "C" int fdgpu_velocity_to_slowness(fdgpu_ctx *ctx, const float *v, float 
 {
     if (!ctx || (!v && n) || (!s && n) || n < 0) return FDGPU_EINVAL;
     cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+    FdDeviceScope dev_(ctx->device);
+    FD_CU(ctx, dev_.err);
     FD_CU(ctx, fdk_launch_v2s(v, s, n, st));
     return FDGPU_OK;
 }
@@ -405,11 +410,32 @@ void record_time(fdgpu_ctx *ctx, const fdgpu_station &s, long long ns)
     else it->second = (it->second + ns) / 2;
 }
 
-/* The public statistics of n solves from their device records (queued on cs, then waited for).
- * Clean solves' times go into the context's launch-order table (st: the stations, in the caller's
- * order). */
+/* which run a set of statistics records comes from: the latest start among them (the GPU's global
+ * timer), different for every run */
+long long run_id(const std::vector<fd_station_stats> &hst)
+{
+    long long id = 0;
+    for (const auto &x : hst) id = std::max(id, (long long)x.t_start_ns);
+    return id;
+}
+
+/* Clean solves' times of one run into the context's launch-order table (st: the stations, in the
+ * caller's order), once per run: *recorded (if given) holds the run last recorded. */
+void record_run(fdgpu_ctx *ctx, const std::vector<fd_station_stats> &hst, const fdgpu_station *st,
+                long long *recorded)
+{
+    const long long id = run_id(hst);
+    if (!st || (recorded && *recorded == id)) return;
+    if (recorded) *recorded = id;
+    for (size_t k = 0; k < hst.size(); k++)
+        if (!hst[k].status && hst[k].t_end_ns > hst[k].t_start_ns)
+            record_time(ctx, st[k], hst[k].t_end_ns - hst[k].t_start_ns);
+}
+
+/* The public statistics of n solves from their device records (queued on cs, then waited for);
+ * their times go into the launch-order table (see record_run). */
 int read_stats(fdgpu_ctx *ctx, const DevBuf &stats_buf, int n, fdgpu_stats *stats, cudaStream_t cs,
-               const fdgpu_station *st)
+               const fdgpu_station *st, long long *recorded)
 {
     std::vector<fd_station_stats> hst(n);
     FD_CU(ctx, cudaMemcpyAsync(hst.data(), stats_buf.p, sizeof(fd_station_stats) * n, cudaMemcpyDeviceToHost, cs));
@@ -418,9 +444,8 @@ int read_stats(fdgpu_ctx *ctx, const DevBuf &stats_buf, int n, fdgpu_stats *stat
     for (int k = 0; k < n; k++) {
         if (stats) fdh::copy_stats(stats[k], hst[k]);
         if (hst[k].status && rc == FDGPU_OK) rc = FDGPU_ESCHED;
-        if (st && !hst[k].status && hst[k].t_end_ns > hst[k].t_start_ns)
-            record_time(ctx, st[k], hst[k].t_end_ns - hst[k].t_start_ns);
     }
+    record_run(ctx, hst, st, recorded);
     return rc;
 }
 
@@ -433,6 +458,7 @@ struct fdgpu_batch {
     long long max_pad = 16;
     long long smem_bytes = 0;   /* launch shape, fixed at creation */
     int csz = 1;
+    long long recorded = -1;    /* the run whose times the order table holds (see record_run) */
     BatchBufs bufs;
 };
 
@@ -442,14 +468,15 @@ extern "C" int fdgpu_solve_device(fdgpu_ctx *ctx, int n, const fdgpu_station *st
 {
     if (!ctx || n < 0 || (n > 0 && (!st || !slowness || !d_times))) return FDGPU_EINVAL;
     if (n == 0) return FDGPU_OK;
-    FD_CU(ctx, cudaSetDevice(ctx->device));
+    FdDeviceScope dev_(ctx->device);
+    FD_CU(ctx, dev_.err);
     cudaStream_t cs = stream ? (cudaStream_t)stream : ctx->stream;
     BatchBufs &bufs = ctx->batch;
     long long max_pad = 16;
     int rc = prepare_batch(ctx, n, st, slowness, s_sy, s_sz, d_times, times_initialised, bufs, cs, &max_pad);
     if (rc == FDGPU_OK) {
         const cudaError_t e = fdk_launch_solve(bufs.stations.as<fd_station_dev>(), n, max_pad, ctx->cluster, cs);
-        rc = e ? cuda_fail(ctx, e, "fdk_launch_solve") : read_stats(ctx, bufs.stats, n, stats, cs, st);
+        rc = e ? cuda_fail(ctx, e, "fdk_launch_solve") : read_stats(ctx, bufs.stats, n, stats, cs, st, nullptr);
     }
     return rc;
 }
@@ -461,7 +488,8 @@ extern "C" int fdgpu_batch_create(fdgpu_ctx *ctx, int n, const fdgpu_station *st
     if (!out) return FDGPU_EINVAL;
     *out = nullptr;
     if (!ctx || n < 1 || !st || !slowness || !d_times) return FDGPU_EINVAL;
-    FD_CU(ctx, cudaSetDevice(ctx->device));
+    FdDeviceScope dev_(ctx->device);
+    FD_CU(ctx, dev_.err);
     auto *b = new (std::nothrow) fdgpu_batch;
     if (!b) return FDGPU_ENOMEM;
     b->ctx = ctx;
@@ -486,6 +514,8 @@ extern "C" int fdgpu_batch_run(fdgpu_batch *b, void *stream)
     if (!b) return FDGPU_EINVAL;
     fdgpu_ctx *ctx = b->ctx;
     cudaStream_t cs = stream ? (cudaStream_t)stream : ctx->stream;
+    FdDeviceScope dev_(ctx->device);   /* switches nothing when the device is already current */
+    FD_CU(ctx, dev_.err);
     FD_CU(ctx, fdk_solve_launch(b->bufs.stations.as<fd_station_dev>(), b->n, b->smem_bytes, b->csz, cs));
     return FDGPU_OK;
 }
@@ -495,7 +525,7 @@ extern "C" int fdgpu_batch_stats(fdgpu_batch *b, fdgpu_stats *stats, void *strea
     if (!b) return FDGPU_EINVAL;
     fdgpu_ctx *ctx = b->ctx;
     return read_stats(ctx, b->bufs.stats, b->n, stats, stream ? (cudaStream_t)stream : ctx->stream,
-                      b->stations.data());
+                      b->stations.data(), &b->recorded);
 }
 
 namespace {
@@ -559,13 +589,12 @@ extern "C" int fdgpu_batch_tune_order(fdgpu_batch *b, void *stream)
     FD_CU(ctx, cudaStreamSynchronize(cs));
     for (int k = 0; k < b->n; k++)
         if (hst[k].t_end_ns <= hst[k].t_start_ns || hst[k].status) return FDGPU_EINVAL;   /* no clean run yet */
-    /* the last run's times into the context's table (blended with earlier ones), then longest first
-     * by the table; equal times keep the current order */
+    /* the last run's times into the context's table (blended with earlier ones, unless
+     * fdgpu_batch_stats already put them there), then longest first by the table; equal times keep
+     * the current order */
+    record_run(ctx, hst, b->stations.data(), &b->recorded);
     std::vector<long long> t(b->n);
-    for (int k = 0; k < b->n; k++) {
-        record_time(ctx, b->stations[k], hst[k].t_end_ns - hst[k].t_start_ns);
-        t[k] = ctx->solve_ns[station_key(b->stations[k])];
-    }
+    for (int k = 0; k < b->n; k++) t[k] = ctx->solve_ns[station_key(b->stations[k])];
     std::vector<fd_station_dev> rec;
     std::vector<int> idx;
     int rc = batch_records(b, rec, idx, cs);
@@ -578,7 +607,7 @@ extern "C" int fdgpu_batch_tune_order(fdgpu_batch *b, void *stream)
 extern "C" void fdgpu_batch_destroy(fdgpu_batch *b)
 {
     if (!b) return;
-    cudaSetDevice(b->ctx->device);
+    FdDeviceScope dev_(b->ctx->device);
     delete b;   /* frees its device buffers */
 }
 
@@ -588,7 +617,8 @@ extern "C" int fdgpu_solve_host(fdgpu_ctx *ctx, int n, const fdgpu_station *st, 
 {
     if (!ctx || n < 0 || (n > 0 && (!st || !velocity || !times)) || mnx < 1 || mny < 1 || mnz < 1) return FDGPU_EINVAL;
     if (n == 0) return FDGPU_OK;
-    FD_CU(ctx, cudaSetDevice(ctx->device));
+    FdDeviceScope dev_(ctx->device);
+    FD_CU(ctx, dev_.err);
     for (int k = 0; k < n; k++) {
         const fdgpu_station &s = st[k];
         if (s.ox < 0 || s.oy < 0 || s.oz < 0 || s.ox + s.nx > mnx || s.oy + s.ny > mny || s.oz + s.nz > mnz)

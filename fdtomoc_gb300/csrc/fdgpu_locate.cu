@@ -31,6 +31,7 @@
 #include <stdint.h>
 
 #include "fdgpu.h"
+#include "fdgpu_device.h"
 
 namespace {
 
@@ -561,7 +562,8 @@ extern "C" int fdgpu_locate(fdgpu_ctx *ctx, const fdgpu_loc_grid *g, const float
         if (o.field < 0 || o.field >= nfields || !d_fields[o.field]) return FDGPU_EINVAL;
         if (o.phase != 'P' && o.phase != 'S') return FDGPU_EINVAL;
     }
-    if (cudaSetDevice(fdh_ctx_device(ctx)) != cudaSuccess) return FDGPU_ENODEV;
+    FdDeviceScope dev_(fdh_ctx_device(ctx));
+    if (dev_.err) return FDGPU_ENODEV;
     cudaStream_t st = stream ? (cudaStream_t)stream : (cudaStream_t)fdh_ctx_stream(ctx);
 
     std::vector<LocObsDev> hobs(nobs);

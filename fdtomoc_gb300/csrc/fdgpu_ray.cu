@@ -22,6 +22,7 @@
 
 #include "../../include/fdgpu.h"
 #include "fd_trig.h"
+#include "fdgpu_device.h"
 
 extern "C" int fdh_ctx_device(const fdgpu_ctx *ctx);
 extern "C" void *fdh_ctx_stream(const fdgpu_ctx *ctx);
@@ -655,7 +656,8 @@ extern "C" int fdgpu_raytrace(fdgpu_ctx *ctx, const fdgpu_ray_grid *g, const flo
         if (obs[k].field < 0 || obs[k].field >= nfields || !d_fields[obs[k].field]) return FDGPU_EINVAL;
     off[0] = 0;
     if (nobs == 0) return FDGPU_OK;
-    if (cudaSetDevice(fdh_ctx_device(ctx)) != cudaSuccess) return FDGPU_ENODEV;
+    FdDeviceScope dev_(fdh_ctx_device(ctx));
+    if (dev_.err) return FDGPU_ENODEV;
     cudaStream_t st = stream ? (cudaStream_t)stream : (cudaStream_t)fdh_ctx_stream(ctx);
 
     /* launch order: longest rays first (cells between event and station), so that a warp's rays end

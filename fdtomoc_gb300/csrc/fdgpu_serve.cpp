@@ -36,6 +36,7 @@
 #include <tuple>
 #include <vector>
 
+#include "fdgpu_device.h"
 #include "fdgpu_layout.h"
 #include "fdgpu_station.h"
 
@@ -728,6 +729,8 @@ extern "C" int fdgpu_serve_open(int device, const fdgpu_serve_opts *opts, fdgpu_
     *out = nullptr;
     int n = 0;
     if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n) return FDGPU_ENODEV;
+    FdDeviceScope dev_(device);
+    if (dev_.err) return FDGPU_ENODEV;
     auto *sv = new (std::nothrow) fdgpu_server;
     if (!sv) return FDGPU_ENOMEM;
     const int rc = sv->open(device, opts);
@@ -754,7 +757,7 @@ extern "C" int fdgpu_serve_set_model(fdgpu_server *sv, int model, const float *v
     if (!sv || !velocity || model < 0 || model >= (int)sv->models.size() || mnx < 1 || mny < 1 || mnz < 1)
         return FDGPU_EINVAL;
     if (((uintptr_t)velocity & 3u) != 0) return FDGPU_EINVAL;
-    cudaSetDevice(sv->device);
+    FdDeviceScope dev_(sv->device);
     int kind = kPageable;
     if (pointer_kind(velocity, sv->device, &kind)) return FDGPU_EINVAL;
     const long long nm = (long long)mnx * mny * mnz;
@@ -808,7 +811,7 @@ extern "C" int fdgpu_serve_submit(fdgpu_server *sv, const fdgpu_station *st, int
     if (rc) return rc;
     if (((uintptr_t)times & 3u) != 0 || ((uintptr_t)init_times & 3u) != 0) return FDGPU_EINVAL;
     if (st->srctype != 1 && !init_times) return FDGPU_EINVAL;
-    cudaSetDevice(sv->device);
+    FdDeviceScope dev_(sv->device);
     auto r = std::make_unique<Req>();
     if (pointer_kind(times, sv->device, &r->out_kind)) return FDGPU_EINVAL;
     if (init_times && pointer_kind(init_times, sv->device, &r->init_kind)) return FDGPU_EINVAL;
@@ -928,6 +931,7 @@ extern "C" int fdgpu_serve_close(fdgpu_server *sv)
     sv->cv_work.notify_all();
     if (sv->thr.joinable()) sv->thr.join();
     const int rc = sv->fatal ? FDGPU_ECUDA : FDGPU_OK;
+    FdDeviceScope dev_(sv->device);
     sv->free_all();
     delete sv;
     return rc;

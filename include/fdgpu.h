@@ -23,6 +23,10 @@
  * caller owns host buffers and any device buffers it passes in; the library owns its scratch,
  * geometry tables and streams, all held in an fdgpu_ctx.  A context is not thread-safe; use one
  * per host thread.  Grids are x fastest (index nx*ny*z + nx*y + x), as in the reference.
+ * Devices: a context, a batch, a c2f plan and a serving session belong to one device; their
+ * calls run there and give the calling thread's current device back as they found it.  The
+ * entry points without such an object (the drop-ins, fdgpu_solve_noalloc) use the calling
+ * thread's current device.
  */
 #ifndef FDGPU_H
 #define FDGPU_H
@@ -163,7 +167,8 @@ int fdgpu_batch_order(fdgpu_batch *batch, int *order, void *stream);
 
 /* The context's launch-order table: every clean solve of fdgpu_solve_device / fdgpu_solve_host /
  * fdgpu_batch_stats records each station's measured solve time (the mean of the new time and the
- * one recorded before), and a later batch whose stations all have one is launched longest first
+ * one recorded before; a batch run's times are recorded once, however often its statistics are
+ * read or its order tuned), and a later batch whose stations all have one is launched longest first
  * (otherwise largest grid first).  order_save writes the table to a file and order_load merges one
  * into the context, so that a new process (the next inversion iteration, say) starts with the
  * order the last one measured.  Results never depend on it.  No counterpart in the reference. */

@@ -212,3 +212,36 @@ def test_order_table_saved_and_loaded(gpu_lib, tmp_path):
         b.close()
         with pytest.raises(lib.FdgpuError):
             ctx.load_order(str(tmp_path / "missing.bin"))
+
+
+def test_batch_run_recorded_once(gpu_lib, tmp_path):
+    """A batch run's times enter the order table once: reading the statistics again, or tuning the
+    order after reading them, leaves the table as the first read left it."""
+    import torch
+    lib = gpu_lib
+    st0, vel = _cases(lib, tmp_path, range(1, 60))[0]
+    nz, ny, nx = vel.shape
+    wins = []
+    for k in range(4):
+        w = lib.Station.from_buffer_copy(st0)
+        w.ox, w.oy = k % 2, k // 2
+        w.nx, w.ny = nx - w.ox - (k % 3), ny - w.oy
+        w.xs, w.ys = min(st0.xs, w.nx - 1), min(st0.ys, w.ny - 1)
+        wins.append(w)
+    with lib.Context(0) as ctx:
+        slow = _slowness(ctx, vel)
+        outs = [torch.empty((w.nz, w.ny, w.nx), dtype=torch.float32, device="cuda") for w in wins]
+        b = lib.Batch(ctx, wins, slow.data_ptr(), nx, nx * ny, [o.data_ptr() for o in outs])
+        tables = []
+        for run in range(2):
+            b.run()
+            b.stats()
+            ctx.save_order(str(tmp_path / f"run{run}.bin"))
+            tables.append((tmp_path / f"run{run}.bin").read_bytes())
+        b.stats()
+        ctx.save_order(str(tmp_path / "again.bin"))
+        b.tune_order()
+        ctx.save_order(str(tmp_path / "tuned.bin"))
+        b.close()
+    assert (tmp_path / "again.bin").read_bytes() == tables[1]
+    assert (tmp_path / "tuned.bin").read_bytes() == tables[1]
