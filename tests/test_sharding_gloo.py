@@ -13,7 +13,7 @@ import torch.multiprocessing as mp
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def _sphfd_worker(rank, world, port, d, q):
+def _sphfd_worker(rank, world, port, d, q, write):
     """One rank of the sharded sphfd driver, with the oracle as its solver."""
     sys.path.insert(0, ROOT)
     sys.path.insert(0, os.path.join(ROOT, "tests"))
@@ -30,15 +30,16 @@ def _sphfd_worker(rank, world, port, d, q):
         solved.extend(entries)
         return [0] * len(entries)
 
-    st = driver.run_spec(os.path.join(d, "spec"), oracle_solver)
+    st = driver.run_spec(os.path.join(d, "spec"), oracle_solver, write=write)
     q.put((rank, st, solved))
     dist.destroy_process_group()
 
 
-def test_two_ranks_solve_a_parlist(tmp_path):
-    """sphfd's driver over two ranks: each solves every other par file (P and S of four stations),
-    rank 0 alone writes the time files into the shared timedir, and they are the reference binary's
-    files byte for byte (tests/golden/reference_outputs.json)."""
+@pytest.mark.parametrize("write", ["each", "rank0"])
+def test_two_ranks_solve_a_parlist(tmp_path, write):
+    """sphfd's driver over two ranks: each solves every other par file (P and S of four stations);
+    the time files in the timedir, written by each rank for its own stations or sent to rank 0 and
+    written there, are the reference binary's files byte for byte (tests/golden/reference_outputs.json)."""
     import hashlib
     import json
     from cases import ps_station_case
@@ -49,7 +50,8 @@ def test_two_ranks_solve_a_parlist(tmp_path):
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
     port = 29500 + os.getpid() % 1000
-    ps = [ctx.Process(target=_sphfd_worker, args=(r, 2, port, str(tmp_path), q)) for r in range(2)]
+    port += 0 if write == "each" else 7
+    ps = [ctx.Process(target=_sphfd_worker, args=(r, 2, port, str(tmp_path), q, write)) for r in range(2)]
     for p in ps:
         p.start()
     got = sorted(q.get(timeout=300) for _ in range(2))
