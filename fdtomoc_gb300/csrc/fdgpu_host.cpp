@@ -212,6 +212,7 @@ extern "C" const char *fdgpu_strerror(int s)
     case FDGPU_ESCHED: return "a schedule check of the solve failed (fdgpu_stats.detail says which)";
     case FDGPU_ENODEV: return "no CUDA device";
     case FDGPU_ETOOBIG: return "problem exceeds the memory the entry point may use";
+    case FDGPU_ETIMEDOUT: return "time limit passed before the wait ended";
     default: return "unknown status";
     }
 }

@@ -873,7 +873,7 @@ extern "C" int fdgpu_serve_drain(fdgpu_server *sv, int timeout_ms)
         sv->cv_done.wait(lk, idle);
         return FDGPU_OK;
     }
-    return sv->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), idle) ? FDGPU_OK : FDGPU_ECUDA;
+    return sv->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), idle) ? FDGPU_OK : FDGPU_ETIMEDOUT;
 }
 
 extern "C" int fdgpu_serve_metrics_get(fdgpu_server *sv, fdgpu_serve_metrics *m)

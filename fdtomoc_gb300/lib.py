@@ -17,7 +17,7 @@ LIB_PATH = os.environ.get("FDGPU_LIB") or os.path.join(HERE, "libfdgpu.so")
 FDGPU_OK = 0
 FDGPU_ETOOBIG = -9
 ERRORS = {-1: "EINVAL", -2: "ENOMEM", -3: "ECUDA", -4: "EIO", -5: "EPAR", -6: "ESOURCE", -7: "ESCHED", -8: "ENODEV",
-          -9: "ETOOBIG"}
+          -9: "ETOOBIG", -10: "ETIMEDOUT"}
 
 
 class Station(C.Structure):

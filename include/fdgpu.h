@@ -48,8 +48,9 @@ enum {
     FDGPU_ESOURCE = -6,  /* the source is outside the grid (src/sphfd.c:533-538) */
     FDGPU_ESCHED = -7,   /* internal: a walk's schedule check failed (fdgpu_stats.detail says which) */
     FDGPU_ENODEV = -8,   /* no CUDA device */
-    FDGPU_ETOOBIG = -9   /* the problem needs more memory than the entry point may use
+    FDGPU_ETOOBIG = -9,  /* the problem needs more memory than the entry point may use
                             (fdgpu_solve_noalloc's static scratch, a serving session's memory) */
+    FDGPU_ETIMEDOUT = -10   /* a wait's time limit passed first (fdgpu_serve_drain) */
 };
 
 typedef struct fdgpu_ctx fdgpu_ctx;
@@ -92,7 +93,11 @@ typedef struct {
                                  releases, 4 sweep bound, 6 a pipelined sweep met a point needing an
                                  earlier point's stencil state, 8 a worker waited too long, 9 a
                                  claimed queue entry was never written, 10 a node queued twice,
-                                 18 a queue entry outside the walk's nodes */
+                                 11 a second point waiting on one point, 12 a point found no
+                                 earlier point to take its stencil state from, 14 a node that no
+                                 face instance owns, 15 a wait table full, 17 a walk ran past its
+                                 bound, 18 a queue entry outside the walk's nodes, 100 + k a
+                                 cluster barrier k gave up (several CTAs per station only) */
     int32_t sm;               /* the SM whose CTA ran the solve */
     int32_t pad;
 } fdgpu_stats;
@@ -288,8 +293,8 @@ int fdgpu_serve_submit(fdgpu_server *sv, const fdgpu_station *st, int model, flo
  * outstanding). */
 int fdgpu_serve_poll(fdgpu_server *sv, fdgpu_serve_result *out, int max, int timeout_ms, int *n);
 
-/* Wait until every submitted request has completed (timeout_ms -1: no limit).  FDGPU_ECUDA if the
- * limit passed first. */
+/* Wait until every submitted request has completed (timeout_ms -1: no limit).  FDGPU_ETIMEDOUT if
+ * the limit passed first; the requests go on, and a later drain or poll collects them. */
 int fdgpu_serve_drain(fdgpu_server *sv, int timeout_ms);
 
 int fdgpu_serve_metrics_get(fdgpu_server *sv, fdgpu_serve_metrics *m);

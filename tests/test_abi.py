@@ -24,6 +24,20 @@ def test_exports_every_declared_function(gpu_lib):
         assert hasattr(lib, n), n
 
 
+def test_every_status_has_a_name_and_a_text(gpu_lib):
+    """Each FDGPU_* status of include/fdgpu.h has its own fdgpu_strerror text and a name in the
+    Python binding's table."""
+    src = open(os.path.join(ROOT, "include", "fdgpu.h")).read()
+    codes = {int(v): n for n, v in re.findall(r"\b(FDGPU_E\w+)\s*=\s*(-?\d+)", src)}
+    assert len(codes) >= 10
+    lib = C.CDLL(gpu_lib.LIB_PATH)
+    lib.fdgpu_strerror.restype = C.c_char_p
+    texts = {lib.fdgpu_strerror(v).decode() for v in codes}
+    assert "unknown status" not in texts and len(texts) == len(codes)
+    for v, n in codes.items():
+        assert gpu_lib.ERRORS[v] == n[len("FDGPU_"):]
+
+
 def test_no_device_is_an_error_not_a_fallback(gpu_lib):
     try:
         import torch
